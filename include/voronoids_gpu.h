@@ -1,0 +1,172 @@
+/* voronoids_gpu.h -- C ABI of the GB300 Delaunay build.
+ *
+ * Drop-in boundary for the `DelaunayTree` new / insert / parallel-insert path
+ * of kazewong/Voronoids.  Each entry point names the reference interface it
+ * replaces (file:line in the reference crate).  Plain pointers and sizes only;
+ * every call returns a vd_status (no panics, no aborts).
+ *
+ * Conventions
+ *  - Points are row-major doubles, `dim` per point (dim = 2 or 3), as the
+ *    reference's Vec<[f64; N]>.  Host pointers unless the name says _device.
+ *  - Vertices are numbered by input order across all insert calls on a tree
+ *    (0, 1, 2, ...); the super-simplex vertices are not part of any output.
+ *  - Edge lists are (u, v) pairs of those vertex numbers with u < v, sorted
+ *    lexicographically.
+ *  - One tree = one CUDA stream; a tree is not thread-safe, distinct trees are.
+ *  - Exactness: conflict tests are exact; a point exactly on a circumsphere is
+ *    resolved by a symbolic perturbation that reproduces the reference's
+ *    strict `dist < r` rule for insertion in input order, so the output is the
+ *    unique triangulation that rule yields, whatever the parallel order.
+ */
+#ifndef VORONOIDS_GPU_H
+#define VORONOIDS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct vd_tree vd_tree;
+
+/* Status codes.  VD_ERR_DUPLICATE is not fatal: duplicates are skipped and the
+ * tree holds the triangulation of the distinct points. */
+enum vd_status {
+  VD_OK = 0,
+  VD_ERR_ARG = 1,          /* bad argument (dim, size, NULL pointer, capacity) */
+  VD_ERR_CUDA = 2,         /* CUDA runtime error */
+  VD_ERR_NOMEM = 3,        /* device allocation failed */
+  VD_ERR_DUPLICATE = 4,    /* some points equal earlier ones and were skipped */
+  VD_ERR_NONFINITE = 5,    /* NaN or infinite coordinate */
+  VD_ERR_OUTSIDE = 6,      /* point not strictly inside the super simplex */
+  VD_ERR_PRECISION = 7,    /* exact-arithmetic capacity exceeded */
+  VD_ERR_ROUND_LIMIT = 8,  /* insertion rounds stopped making progress */
+  VD_ERR_CAVITY = 9,       /* a conflict region exceeded the supported size */
+  VD_ERR_WALK = 10,        /* point location did not terminate */
+  VD_ERR_INTERNAL = 11,    /* inconsistent internal state */
+  VD_ERR_DEGENERATE = 12,  /* super simplex degenerate (e.g. all points equal) */
+  VD_ERR_RANGE = 13        /* |coordinate| outside [2^-150, 2^150] (and not 0) */
+};
+
+typedef struct vd_stats {
+  int64_t rounds;            /* insertion rounds run on this tree */
+  int64_t inserted;          /* vertices inserted */
+  int64_t duplicates;        /* points skipped as duplicates */
+  int64_t live_simplices;    /* simplices of the current triangulation (incl. super) */
+  int64_t slots;             /* simplex slots in use (live + holes) */
+  int64_t created;           /* simplices created over all insertions */
+  int64_t killed;            /* simplices removed over all insertions */
+  int64_t max_cavity;        /* largest conflict region (simplices) */
+  int64_t max_facets;        /* largest conflict-region boundary (facets) */
+  int64_t pred_f32;          /* predicates decided by the FP32 filter */
+  int64_t pred_f64;          /* ... by the FP64 filter */
+  int64_t pred_exact;        /* ... by exact expansion arithmetic */
+  int64_t pred_sos;          /* ... of which resolved by symbolic perturbation */
+  int64_t walk_steps;        /* point-relocation steps */
+  int64_t cavity_tests;      /* conflict tests during cavity searches */
+  int64_t deferred_overflow; /* candidate deferrals: cavity above per-warp capacity */
+  int64_t deferred_pool;     /* candidate deferrals: cavity pool full */
+  int64_t candidates;        /* nominations (one per simplex holding points, per round) */
+  int64_t searched;          /* nominations that won the thinning claim and were searched */
+  int64_t won_pass[3];       /* insertions decided in resolution pass 0, 1, 2 and later */
+  int64_t spilled;           /* cavity searches that spilled to the pool */
+} vd_stats;
+
+/* DelaunayTree::<3,4>::new / ::<2,3>::new
+ * (src/delaunay_tree.rs:389-510, :544-640; bounding_sphere src/geometry.rs:99-142).
+ * Sizes the super simplex from `pts` (n points); the points are NOT inserted.
+ * Returns NULL only if allocation of the handle itself fails; otherwise check
+ * *status. */
+vd_tree* vd_tree_new(int dim, const double* pts, int64_t n, int* status);
+/* Same, with all device work on the caller's CUDA stream (cudaStream_t). */
+vd_tree* vd_tree_new_on_stream(int dim, const double* pts, int64_t n, void* stream, int* status);
+void vd_tree_free(vd_tree* t);
+
+/* The super simplex `new` would build for `pts` (host computation only, no
+ * device work): out[3*k + j] = coordinate j of super vertex k (z = 0 in 2D),
+ * in the reference's vertex order, and *radius = 10 x bounding radius.
+ * bounding_sphere src/geometry.rs:99-142; vertices src/delaunay_tree.rs:392-406,
+ * :547-558. */
+int vd_super_simplex(int dim, const double* pts, int64_t n, double* out, double* radius);
+
+/* DelaunayTree::add_points_to_tree (src/delaunay_tree.rs:336-386), with the
+ * queue/placement of src/scheduler.rs:6-55 replaced by GPU priority rounds.
+ * `seed` fixes the random insertion priorities. */
+int vd_insert_points(vd_tree* t, const double* pts, int64_t n, uint64_t seed);
+/* Same with `d_pts` already in device memory (n * dim doubles). */
+int vd_insert_points_device(vd_tree* t, const double* d_pts, int64_t n, uint64_t seed);
+/* TreeUpdate::new + DelaunayTree::insert_point
+ * (src/delaunay_tree.rs:709-740, :125-211): one point. */
+int vd_insert_point(vd_tree* t, const double* p);
+
+/* Conflict region of a query point (`locate`, src/delaunay_tree.rs:33-58):
+ * ids of the simplices whose circumsphere strictly contains `p` (perturbed),
+ * sorted ascending.  *n receives the count even when it exceeds `cap`. */
+int vd_locate(vd_tree* t, const double* p, int64_t* out, int64_t cap, int64_t* n);
+
+/* Vertices inserted so far (super vertices excluded). */
+int vd_num_vertices(vd_tree* t, int64_t* n);
+/* DelaunayTree::max_simplex_id (src/delaunay_tree.rs:29): id of the last
+ * simplex created, counting the reference's initial 5 (3D) / 4 (2D). */
+int vd_max_simplex_id(vd_tree* t, int64_t* id);
+
+/* Live simplices, as the reference's simplex map (src/lib.rs:142-156):
+ * verts[4*i + j] = vertex j of simplex i (super vertices are -(1+k), k = 0..dim;
+ * in 2D verts[4*i+3] = -1); nbrs[4*i + j] = simplex across the face opposite
+ * vertex j, or -1 on the hull.  *n receives the count. */
+int vd_num_simplices(vd_tree* t, int64_t* n);
+int vd_simplices(vd_tree* t, int32_t* verts, int32_t* nbrs, int64_t cap, int64_t* n);
+
+/* Sorted Delaunay edge list among inserted points. */
+int vd_num_edges(vd_tree* t, int64_t* n);
+int vd_edges(vd_tree* t, int64_t* uv, int64_t cap, int64_t* n);
+/* Same into device memory as uint32 pairs. */
+int vd_edges_device(vd_tree* t, uint32_t* d_uv, int64_t cap, int64_t* n);
+
+/* DelaunayTree::check_delaunay (src/delaunay_tree.rs:512-541, :642-671),
+ * exact: *ok = 1 iff every simplex is positively oriented, adjacency is
+ * symmetric and every interior facet is locally Delaunay.  `violations`
+ * (NULL or 6 entries): non-positive, asymmetric, not Delaunay, not
+ * perturbed-Delaunay, hull facets, facets checked. */
+int vd_check_delaunay(vd_tree* t, int* ok, int64_t* violations);
+
+/* Duplicates skipped so far: pairs (skipped vertex, vertex it equals). */
+int vd_duplicates(vd_tree* t, int64_t* pairs, int64_t cap, int64_t* n);
+
+int vd_get_stats(vd_tree* t, vd_stats* s);
+const char* vd_status_str(int status);
+
+/* Diagnostics (no reference counterpart; the reference prints timings with
+ * println!, src/delaunay_tree.rs:337-368).  Profiling records CUDA events
+ * around every kernel of every round on the tree's stream; vd_profile returns
+ * the summed milliseconds and launch counts per kernel (names from
+ * vd_profile_name; the last entry is the edge extraction).  Turning it on
+ * resets the sums.  The trace synchronises after every round and keeps one
+ * row per round: round, active points at start, cumulative nominations,
+ * cumulative searches, cumulative insertions, cumulative conflict tests,
+ * cumulative walk steps, active points after the round. */
+int vd_set_profiling(vd_tree* t, int on);
+/* Insertion schedule (no reference counterpart: the reference inserts all of
+ * a batch against one queue, src/scheduler.rs:6-55): points are inserted in
+ * priority prefixes of `first_prefix` points, then growing by `growth` (>= 1.5)
+ * per prefix.  Defaults 64 and 4. */
+int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth);
+/* Round tuning: resolution passes per round (1..6, default 3) and the
+ * thinning radius (1 = a nominee must hold its simplex and face neighbours,
+ * 2 = and no lower nominee two faces away; default 1). */
+int vd_set_tuning(vd_tree* t, int passes, int thin);
+int vd_profile(vd_tree* t, double* ms, int64_t* launches, int cap, int* n);
+const char* vd_profile_name(int i);
+int vd_set_trace(vd_tree* t, int on);
+int vd_trace(vd_tree* t, int64_t* rows, int64_t cap, int64_t* n);
+
+/* voronoids.delaunay(points) (src/lib.rs:104-125) in one call: new + insert
+ * all points + sorted edge list.  `uv` may be NULL to query the count. */
+int vd_delaunay(int dim, const double* pts, int64_t n, uint64_t seed, int64_t* uv, int64_t cap,
+                int64_t* n_edges);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VORONOIDS_GPU_H */

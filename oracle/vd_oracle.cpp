@@ -1,0 +1,916 @@
+// CPU oracle for the GB300 Delaunay build -- TEST INFRASTRUCTURE ONLY.
+//
+// Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
+// this library.  It restates, sequentially and with exact arithmetic, the
+// semantics of the reference crate kazewong/Voronoids:
+//
+//   bounding_sphere            src/geometry.rs:99-142     (bit-exact restatement)
+//   DelaunayTree<3,4>::new     src/delaunay_tree.rs:389-510 (super vertices)
+//   DelaunayTree<2,3>::new     src/delaunay_tree.rs:544-640
+//   circumsphere_2d / _3d      src/geometry.rs:2-56       (float variant, diagnostics)
+//   in_sphere (strict)         src/geometry.rs:91-97      (exact + strict)
+//   locate / find_all_neighbors src/delaunay_tree.rs:33-75 (conflict region by BFS)
+//   get_new_simplices          src/delaunay_tree.rs:77-123 (star from boundary facets)
+//   pair_simplices             src/delaunay_tree.rs:674-695 (intra-star adjacency)
+//   insert_point               src/delaunay_tree.rs:125-211 (apply one insertion)
+//   check_delaunay             src/delaunay_tree.rs:512-541, 642-671 (validator)
+//
+// Differences from the reference, all deliberate:
+//  * predicates are exact (f64 filter, then big-integer arithmetic) instead of
+//    a floating circumcenter; a point exactly on a circumsphere is resolved by
+//    the perturbation rule (larger vertex id = larger lift perturbation),
+//    which equals the reference's strict `<` whenever the query is the newest
+//    vertex, i.e. for its sequential input-order insertion;
+//  * point location walks from the last created simplex instead of the kd-tree
+//    nearest vertex (location picks the start of the BFS only; the conflict
+//    region it finds is the same set);
+//  * duplicate points are skipped (the reference panics, src/delaunay_tree.rs:53);
+//    of a group of equal points the one with the smallest insertion priority
+//    is kept;
+//  * ghost simplices are represented as "no neighbour" (-1) across the
+//    super-simplex hull; they never conflict in the reference either.
+//
+// The big-integer path is written independently of the device code's
+// floating-point expansions so that the two exact methods check each other.
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <map>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Big integers (sign + magnitude, base 2^32).
+// ---------------------------------------------------------------------------
+struct Big {
+  int sign = 0;                 // -1, 0, +1
+  std::vector<uint32_t> mag;    // little endian, no leading zero limbs
+};
+
+void trim(std::vector<uint32_t>& m) {
+  while (!m.empty() && m.back() == 0) m.pop_back();
+}
+
+int cmp_mag(const std::vector<uint32_t>& a, const std::vector<uint32_t>& b) {
+  if (a.size() != b.size()) return a.size() < b.size() ? -1 : 1;
+  for (size_t i = a.size(); i-- > 0;)
+    if (a[i] != b[i]) return a[i] < b[i] ? -1 : 1;
+  return 0;
+}
+
+std::vector<uint32_t> add_mag(const std::vector<uint32_t>& a, const std::vector<uint32_t>& b) {
+  std::vector<uint32_t> r(std::max(a.size(), b.size()) + 1, 0);
+  uint64_t carry = 0;
+  for (size_t i = 0; i < r.size(); ++i) {
+    uint64_t s = carry;
+    if (i < a.size()) s += a[i];
+    if (i < b.size()) s += b[i];
+    r[i] = (uint32_t)s;
+    carry = s >> 32;
+  }
+  trim(r);
+  return r;
+}
+
+// a - b with |a| >= |b|
+std::vector<uint32_t> sub_mag(const std::vector<uint32_t>& a, const std::vector<uint32_t>& b) {
+  std::vector<uint32_t> r(a.size(), 0);
+  int64_t borrow = 0;
+  for (size_t i = 0; i < a.size(); ++i) {
+    int64_t s = (int64_t)a[i] - borrow - (i < b.size() ? (int64_t)b[i] : 0);
+    borrow = 0;
+    if (s < 0) {
+      s += ((int64_t)1 << 32);
+      borrow = 1;
+    }
+    r[i] = (uint32_t)s;
+  }
+  trim(r);
+  return r;
+}
+
+Big badd(const Big& a, const Big& b) {
+  if (a.sign == 0) return b;
+  if (b.sign == 0) return a;
+  Big r;
+  if (a.sign == b.sign) {
+    r.sign = a.sign;
+    r.mag = add_mag(a.mag, b.mag);
+    return r;
+  }
+  int c = cmp_mag(a.mag, b.mag);
+  if (c == 0) return r;
+  if (c > 0) {
+    r.sign = a.sign;
+    r.mag = sub_mag(a.mag, b.mag);
+  } else {
+    r.sign = b.sign;
+    r.mag = sub_mag(b.mag, a.mag);
+  }
+  return r;
+}
+
+Big bneg(Big a) {
+  a.sign = -a.sign;
+  return a;
+}
+Big bsub(const Big& a, const Big& b) { return badd(a, bneg(b)); }
+
+Big bmul(const Big& a, const Big& b) {
+  Big r;
+  if (a.sign == 0 || b.sign == 0) return r;
+  std::vector<uint64_t> acc(a.mag.size() + b.mag.size() + 1, 0);
+  std::vector<uint32_t> m(a.mag.size() + b.mag.size() + 1, 0);
+  for (size_t i = 0; i < a.mag.size(); ++i) {
+    uint64_t carry = 0;
+    for (size_t j = 0; j < b.mag.size(); ++j) {
+      uint64_t cur = (uint64_t)a.mag[i] * b.mag[j] + m[i + j] + carry;
+      m[i + j] = (uint32_t)cur;
+      carry = cur >> 32;
+    }
+    size_t k = i + b.mag.size();
+    while (carry) {
+      uint64_t cur = (uint64_t)m[k] + carry;
+      m[k] = (uint32_t)cur;
+      carry = cur >> 32;
+      ++k;
+    }
+  }
+  trim(m);
+  r.mag = m;
+  r.sign = a.sign * b.sign;
+  return r;
+}
+
+// Exact value x * 2^-emin as a big integer (x = mant * 2^e, e >= emin).
+Big from_double(double x, int emin) {
+  Big r;
+  if (x == 0.0) return r;
+  int k;
+  double f = std::frexp(std::fabs(x), &k);
+  uint64_t m = (uint64_t)std::ldexp(f, 53);
+  int e = k - 53;
+  int sh = e - emin;
+  // m << sh
+  std::vector<uint32_t> mag;
+  int limbs = sh / 32, bits = sh % 32;
+  mag.assign(limbs, 0);
+  unsigned __int128 v = (unsigned __int128)m << bits;
+  while (v) {
+    mag.push_back((uint32_t)v);
+    v >>= 32;
+  }
+  trim(mag);
+  r.mag = mag;
+  r.sign = x > 0 ? 1 : -1;
+  return r;
+}
+
+int low_exponent(double x) {
+  int k;
+  std::frexp(std::fabs(x), &k);
+  return k - 53;
+}
+
+// ---------------------------------------------------------------------------
+// Exact predicates.  Points are given as raw coordinates; differences are
+// formed exactly in big integers after aligning all inputs to a common
+// binary exponent.
+// ---------------------------------------------------------------------------
+struct P3 {
+  double x, y, z;
+};
+
+int emin_of(const P3* p, int n) {
+  int em = 1 << 30;
+  for (int i = 0; i < n; ++i) {
+    const double c[3] = {p[i].x, p[i].y, p[i].z};
+    for (double v : c)
+      if (v != 0.0) em = std::min(em, low_exponent(v));
+  }
+  return em == (1 << 30) ? 0 : em;
+}
+
+// det2 rows (a, b)
+Big bdet2(const Big& ax, const Big& ay, const Big& bx, const Big& by) {
+  return bsub(bmul(ax, by), bmul(ay, bx));
+}
+
+// det3 rows (a, b, c)
+Big bdet3(const Big* x, const Big* y, const Big* z, int a, int b, int c) {
+  Big t1 = bmul(z[a], bdet2(x[b], y[b], x[c], y[c]));
+  Big t2 = bmul(z[b], bdet2(x[a], y[a], x[c], y[c]));
+  Big t3 = bmul(z[c], bdet2(x[a], y[a], x[b], y[b]));
+  return badd(bsub(t1, t2), t3);
+}
+
+// O_i = orient(T with p_i replaced by q) for the simplex p[0..dim], all
+// exactly, plus the exact lifted determinant sum_i |p_i - q|^2 O_i.
+void exact_lifted(int dim, const P3* p, const P3& q, int* osign, int* detsign) {
+  P3 all[5];
+  int nv = dim + 1;
+  for (int i = 0; i < nv; ++i) all[i] = p[i];
+  all[nv] = q;
+  int em = emin_of(all, nv + 1);
+  Big qx = from_double(q.x, em), qy = from_double(q.y, em), qz = from_double(q.z, em);
+  Big x[4], y[4], z[4];
+  for (int i = 0; i < nv; ++i) {
+    x[i] = bsub(from_double(p[i].x, em), qx);
+    y[i] = bsub(from_double(p[i].y, em), qy);
+    z[i] = bsub(from_double(p[i].z, em), qz);
+  }
+  Big det;
+  for (int i = 0; i < nv; ++i) {
+    int o[3], t = 0;
+    for (int k = 0; k < nv; ++k)
+      if (k != i) o[t++] = k;
+    Big Oi;
+    if (dim == 3) {
+      Oi = bdet3(x, y, z, o[0], o[1], o[2]);
+      if (!(i & 1)) Oi = bneg(Oi);
+    } else {
+      Oi = bdet2(x[o[0]], y[o[0]], x[o[1]], y[o[1]]);
+      if (i & 1) Oi = bneg(Oi);
+    }
+    osign[i] = Oi.sign;
+    Big w = badd(bmul(x[i], x[i]), bmul(y[i], y[i]));
+    if (dim == 3) w = badd(w, bmul(z[i], z[i]));
+    det = badd(det, bmul(w, Oi));
+  }
+  *detsign = det.sign;
+}
+
+// orient of (p[0..dim]) in the repository's convention:
+// 3D det[a-d; b-d; c-d], 2D det[a-c; b-c]
+int exact_orient(int dim, const P3* p) {
+  int nv = dim + 1;
+  int em = emin_of(p, nv);
+  const P3& o = p[dim];
+  Big ox = from_double(o.x, em), oy = from_double(o.y, em), oz = from_double(o.z, em);
+  Big x[3], y[3], z[3];
+  for (int i = 0; i < dim; ++i) {
+    x[i] = bsub(from_double(p[i].x, em), ox);
+    y[i] = bsub(from_double(p[i].y, em), oy);
+    z[i] = bsub(from_double(p[i].z, em), oz);
+  }
+  if (dim == 3) return bdet3(x, y, z, 0, 1, 2).sign;
+  return bdet2(x[0], y[0], x[1], y[1]).sign;
+}
+
+// f64 filter for orient; returns 0 when undecided.
+int filter_orient(int dim, const P3* p) {
+  const P3& o = p[dim];
+  double x[3], y[3], z[3];
+  double mx = 0;
+  for (int i = 0; i < dim; ++i) {
+    x[i] = p[i].x - o.x;
+    y[i] = p[i].y - o.y;
+    z[i] = p[i].z - o.z;
+    mx = std::max({mx, std::fabs(x[i]), std::fabs(y[i]), std::fabs(z[i])});
+  }
+  if (!(mx < 1e30)) return 0;
+  double det, perm;
+  if (dim == 3) {
+    double m12 = x[1] * y[2] - y[1] * x[2], p12 = std::fabs(x[1] * y[2]) + std::fabs(y[1] * x[2]);
+    double m02 = x[0] * y[2] - y[0] * x[2], p02 = std::fabs(x[0] * y[2]) + std::fabs(y[0] * x[2]);
+    double m01 = x[0] * y[1] - y[0] * x[1], p01 = std::fabs(x[0] * y[1]) + std::fabs(y[0] * x[1]);
+    det = z[0] * m12 - z[1] * m02 + z[2] * m01;
+    perm = std::fabs(z[0]) * p12 + std::fabs(z[1]) * p02 + std::fabs(z[2]) * p01;
+  } else {
+    det = x[0] * y[1] - y[0] * x[1];
+    perm = std::fabs(x[0] * y[1]) + std::fabs(y[0] * x[1]);
+  }
+  if (!(perm > 1e-150)) return 0;
+  double bound = 32.0 * 1.1102230246251565e-16 * perm;
+  if (det > bound) return 1;
+  if (det < -bound) return -1;
+  return 0;
+}
+
+int orient(int dim, const P3* p, long long* nexact) {
+  int s = filter_orient(dim, p);
+  if (s != 0) return s;
+  if (nexact) ++*nexact;
+  return exact_orient(dim, p);
+}
+
+// Perturbed conflict test: +1 inside, -1 outside (never 0).
+int insphere_sos(int dim, const P3* p, const int* key, const P3& q, int qkey, long long* nexact,
+                 long long* nsos) {
+  int nv = dim + 1;
+  // f64 filter
+  double x[4], y[4], z[4], mx = 0;
+  for (int i = 0; i < nv; ++i) {
+    x[i] = p[i].x - q.x;
+    y[i] = p[i].y - q.y;
+    z[i] = p[i].z - q.z;
+    mx = std::max({mx, std::fabs(x[i]), std::fabs(y[i]), std::fabs(z[i])});
+  }
+  if (mx < 1e30) {
+    double det = 0, perm = 0;
+    for (int i = 0; i < nv; ++i) {
+      int o[3], t = 0;
+      for (int k = 0; k < nv; ++k)
+        if (k != i) o[t++] = k;
+      double Oi, Pi;
+      if (dim == 3) {
+        auto m = [&](int a, int b) { return x[a] * y[b] - y[a] * x[b]; };
+        auto pm = [&](int a, int b) { return std::fabs(x[a] * y[b]) + std::fabs(y[a] * x[b]); };
+        Oi = z[o[0]] * m(o[1], o[2]) - z[o[1]] * m(o[0], o[2]) + z[o[2]] * m(o[0], o[1]);
+        Pi = std::fabs(z[o[0]]) * pm(o[1], o[2]) + std::fabs(z[o[1]]) * pm(o[0], o[2]) +
+             std::fabs(z[o[2]]) * pm(o[0], o[1]);
+        if (!(i & 1)) Oi = -Oi;
+      } else {
+        Oi = x[o[0]] * y[o[1]] - y[o[0]] * x[o[1]];
+        Pi = std::fabs(x[o[0]] * y[o[1]]) + std::fabs(y[o[0]] * x[o[1]]);
+        if (i & 1) Oi = -Oi;
+      }
+      double w = x[i] * x[i] + y[i] * y[i] + z[i] * z[i];
+      det += w * Oi;
+      perm += w * Pi;
+    }
+    if (perm > 1e-150) {
+      double bound = 64.0 * 1.1102230246251565e-16 * perm;
+      if (det > bound) return 1;
+      if (det < -bound) return -1;
+    }
+  }
+  if (nexact) ++*nexact;
+  int os[4], ds;
+  exact_lifted(dim, p, q, os, &ds);
+  if (ds != 0) return ds;
+  if (nsos) ++*nsos;
+  // perturbation: walk the vertices from the largest key down
+  int order[4];
+  for (int i = 0; i < nv; ++i) order[i] = i;
+  std::sort(order, order + nv, [&](int a, int b) { return key[a] > key[b]; });
+  for (int t = 0; t < nv; ++t) {
+    int i = order[t];
+    if (key[i] < qkey) return -1;
+    if (os[i] != 0) return os[i];
+  }
+  return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Reference super simplex (bit-exact restatement, host libm cos/sin).
+// ---------------------------------------------------------------------------
+bool rs_in_sphere(const double* v, const double* c, double r, int dim) {
+  double d = 0.0;
+  for (int i = 0; i < dim; ++i) d += (c[i] - v[i]) * (c[i] - v[i]);
+  return d < r * r;
+}
+
+void bounding_sphere(int dim, const double* pts, int64_t n, double* center, double* radius) {
+  double lo[3], hi[3];
+  for (int i = 0; i < dim; ++i) {
+    double l = INFINITY, h = -INFINITY;
+    for (int64_t k = 0; k < n; ++k) {
+      double v = pts[k * dim + i];
+      l = std::fmin(l, v);
+      h = std::fmax(h, v);
+    }
+    lo[i] = l;
+    hi[i] = h;
+    center[i] = (h + l) / 2.0;
+  }
+  double su = 0.0, sl = 0.0;
+  for (int i = 0; i < dim; ++i) su += (hi[i] - center[i]) * (hi[i] - center[i]);
+  for (int i = 0; i < dim; ++i) sl += (lo[i] - center[i]) * (lo[i] - center[i]);
+  double ud = std::sqrt(su), ld = std::sqrt(sl);
+  double r = ud > ld ? ud : ld;
+  for (int64_t k = 0; k < n; ++k) {
+    if (!rs_in_sphere(pts + k * dim, center, r, dim)) r = r * 1.5;
+  }
+  *radius = r;
+}
+
+// out: (dim+1) super vertices, each 3 doubles (z = 0 in 2D), in reference order.
+void super_vertices(int dim, const double* pts, int64_t n, double* out, double* R) {
+  double c[3] = {0, 0, 0}, r;
+  bounding_sphere(dim, pts, n, c, &r);
+  r *= 10.0;
+  *R = r;
+  const double pi = 3.141592653589793;
+  double c1 = std::cos(2. * pi / 3.), s1 = std::sin(2. * pi / 3.);
+  double c2 = std::cos(4. * pi / 3.), s2 = std::sin(4. * pi / 3.);
+  if (dim == 3) {
+    double v[4][3] = {{c[0], c[1], c[2] + r},
+                      {c[0] + r, c[1], c[2] - r},
+                      {c[0] + r * c1, c[1] + r * s1, c[2] - r},
+                      {c[0] + r * c2, c[1] + r * s2, c[2] - r}};
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 3; ++j) out[i * 3 + j] = v[i][j];
+  } else {
+    double v[3][2] = {{c[0] + r, c[1]}, {c[0] + r * c1, c[1] + r * s1}, {c[0] + r * c2, c[1] + r * s2}};
+    for (int i = 0; i < 3; ++i) {
+      out[i * 3 + 0] = v[i][0];
+      out[i * 3 + 1] = v[i][1];
+      out[i * 3 + 2] = 0.0;
+    }
+  }
+}
+
+// Float variant of the reference circumsphere (src/geometry.rs:2-56): 2D slope
+// formula, 3D Gaussian elimination with partial pivoting.
+void circumsphere_float(int dim, const double* v, double* center, double* radius) {
+  if (dim == 2) {
+    double x1 = v[0], y1 = v[1], x2 = v[2], y2 = v[3], x3 = v[4], y3 = v[5];
+    double d0 = (x1 + x2) / 2.0, d1 = (y1 + y2) / 2.0;
+    double e0 = (x2 + x3) / 2.0, e1 = (y2 + y3) / 2.0;
+    double m_ab = (y2 - y1) / (x2 - x1);
+    double m_bc = (y3 - y2) / (x3 - x2);
+    double m_d = -1. / m_ab, m_e = -1. / m_bc;
+    double x = (m_d * d0 - m_e * e0 + e1 - d1) / (m_d - m_e);
+    double y = m_d * (x - d0) + d1;
+    center[0] = x;
+    center[1] = y;
+    *radius = std::sqrt((x - x1) * (x - x1) + (y - y1) * (y - y1));
+    return;
+  }
+  double A[3][3], b[3];
+  for (int i = 0; i < 3; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < 3; ++j) {
+      A[i][j] = v[(i + 1) * 3 + j] - v[j];
+      double mid = (v[(i + 1) * 3 + j] + v[j]) / 2.0;
+      s += A[i][j] * mid;
+    }
+    b[i] = s;
+  }
+  int piv[3] = {0, 1, 2};
+  for (int k = 0; k < 3; ++k) {
+    int p = k;
+    for (int i = k + 1; i < 3; ++i)
+      if (std::fabs(A[i][k]) > std::fabs(A[p][k])) p = i;
+    if (p != k) {
+      for (int j = 0; j < 3; ++j) std::swap(A[k][j], A[p][j]);
+      std::swap(b[k], b[p]);
+      std::swap(piv[k], piv[p]);
+    }
+    for (int i = k + 1; i < 3; ++i) {
+      double f = A[i][k] / A[k][k];
+      for (int j = k; j < 3; ++j) A[i][j] -= f * A[k][j];
+      b[i] -= f * b[k];
+    }
+  }
+  double xs[3];
+  for (int i = 2; i >= 0; --i) {
+    double s = b[i];
+    for (int j = i + 1; j < 3; ++j) s -= A[i][j] * xs[j];
+    xs[i] = s / A[i][i];
+  }
+  for (int j = 0; j < 3; ++j) center[j] = xs[j];
+  double r2 = 0.0;
+  for (int j = 0; j < 3; ++j) r2 += (v[j] - xs[j]) * (v[j] - xs[j]);
+  *radius = std::sqrt(r2);
+}
+
+// Insertion priority: a bijective 32-bit mix of the vertex id and the seed.
+uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+uint32_t priority(uint32_t vid, uint64_t seed) {
+  uint32_t x = vid ^ (uint32_t)seed;
+  x = mix32(x);
+  x ^= (uint32_t)(seed >> 32);
+  return mix32(x);
+}
+
+// ---------------------------------------------------------------------------
+// Sequential Bowyer-Watson.
+// ---------------------------------------------------------------------------
+struct Simplex {
+  int v[4];
+  int n[4];
+  bool alive;
+};
+
+struct Tree {
+  int dim = 3;
+  int ns = 4;  // number of super vertices
+  std::vector<P3> pts;       // vertex id -> coordinates
+  std::vector<Simplex> s;
+  std::vector<int> dup_of;   // input index -> kept input index, or -1
+  int last = 0;
+  int status = 0;
+  long long nexact = 0, nsos = 0, nwalk = 0, maxcav = 0, maxfac = 0;
+  std::vector<int> mark;     // BFS stamps
+  int stamp = 0;
+};
+
+enum { OK = 0, ERR_ARG = 1, ERR_OUTSIDE = 6, ERR_WALK = 10, ERR_DEGENERATE = 12 };
+
+void simplex_points(const Tree& t, int si, P3* out) {
+  for (int i = 0; i <= t.dim; ++i) out[i] = t.pts[t.s[si].v[i]];
+}
+
+// visibility walk to a simplex whose closed hull contains p
+int locate(Tree& t, const P3& p, int start) {
+  int cur = start;
+  long long cap = 64 + 4 * (long long)t.s.size();
+  for (long long step = 0; step < cap; ++step) {
+    const Simplex& S = t.s[cur];
+    int nv = t.dim + 1, moved = -1;
+    for (int j = 0; j < nv; ++j) {
+      P3 q[4];
+      simplex_points(t, cur, q);
+      q[j] = p;
+      if (orient(t.dim, q, &t.nexact) < 0) {
+        moved = j;
+        break;
+      }
+    }
+    if (moved < 0) return cur;
+    ++t.nwalk;
+    int nb = S.n[moved];
+    if (nb < 0) return -2;  // outside the super simplex
+    cur = nb;
+  }
+  return -1;
+}
+
+int insert_vertex(Tree& t, int vid) {
+  const P3 p = t.pts[vid];
+  int nv = t.dim + 1;
+  int start = t.last;
+  if (!t.s[start].alive) start = 0;
+  while (!t.s[start].alive) ++start;
+  int c0 = locate(t, p, start);
+  if (c0 == -2) return ERR_OUTSIDE;
+  if (c0 < 0) return ERR_WALK;
+  for (int i = 0; i < nv; ++i) {
+    const P3& q = t.pts[t.s[c0].v[i]];
+    if (q.x == p.x && q.y == p.y && q.z == p.z) return ERR_ARG;  // duplicate (pre-filtered)
+  }
+  // conflict region by BFS (locate + find_all_neighbors)
+  if (t.mark.size() < t.s.size()) t.mark.resize(t.s.size() * 2 + 16, 0);
+  ++t.stamp;
+  std::vector<int> cav{c0};
+  t.mark[c0] = t.stamp;
+  struct Facet {
+    int simp, face, outer;
+  };
+  std::vector<Facet> bnd;
+  for (size_t h = 0; h < cav.size(); ++h) {
+    int c = cav[h];
+    for (int f = 0; f < nv; ++f) {
+      int nb = t.s[c].n[f];
+      if (nb < 0) {
+        bnd.push_back({c, f, -1});
+        continue;
+      }
+      if (t.mark[nb] == t.stamp) continue;
+      P3 q[4];
+      simplex_points(t, nb, q);
+      int key[4];
+      for (int i = 0; i < nv; ++i) key[i] = t.s[nb].v[i];
+      if (insphere_sos(t.dim, q, key, p, vid, &t.nexact, &t.nsos) > 0) {
+        t.mark[nb] = t.stamp;
+        cav.push_back(nb);
+      } else {
+        bnd.push_back({c, f, nb});
+      }
+    }
+  }
+  t.maxcav = std::max<long long>(t.maxcav, (long long)cav.size());
+  t.maxfac = std::max<long long>(t.maxfac, (long long)bnd.size());
+  // star: one new simplex per boundary facet (get_new_simplices)
+  int base = (int)t.s.size();
+  t.s.resize(base + bnd.size());
+  // ridge -> (new simplex, face) for intra-star adjacency (pair_simplices)
+  std::map<std::array<int, 2>, std::pair<int, int>> open;
+  for (size_t k = 0; k < bnd.size(); ++k) {
+    const Facet& F = bnd[k];
+    Simplex ns;
+    ns.alive = true;
+    for (int i = 0; i < 4; ++i) {
+      ns.v[i] = (i < nv) ? t.s[F.simp].v[i] : -1;
+      ns.n[i] = -1;
+    }
+    ns.v[F.face] = vid;
+    ns.n[F.face] = F.outer;
+    int id = base + (int)k;
+    if (F.outer >= 0) {
+      Simplex& O = t.s[F.outer];
+      for (int j = 0; j < nv; ++j)
+        if (O.n[j] == F.simp) O.n[j] = id;
+    }
+    for (int g = 0; g < nv; ++g) {
+      if (g == F.face) continue;
+      std::array<int, 2> ridge = {-1, -1};
+      int r = 0;
+      for (int i = 0; i < nv; ++i)
+        if (i != g && i != F.face) ridge[r++] = ns.v[i];
+      if (r == 2 && ridge[0] > ridge[1]) std::swap(ridge[0], ridge[1]);
+      auto it = open.find(ridge);
+      if (it == open.end()) {
+        open[ridge] = {id, g};
+      } else {
+        ns.n[g] = it->second.first;
+        t.s[it->second.first].n[it->second.second] = id;
+        open.erase(it);
+      }
+    }
+    t.s[id] = ns;
+  }
+  if (!open.empty()) return ERR_WALK;
+  for (int c : cav) t.s[c].alive = false;
+  t.last = base;
+  return OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- reference arithmetic restatements -----------------------------------
+void vdo_bounding_sphere(int dim, const double* pts, int64_t n, double* center, double* radius) {
+  bounding_sphere(dim, pts, n, center, radius);
+}
+void vdo_super_vertices(int dim, const double* pts, int64_t n, double* out, double* R) {
+  super_vertices(dim, pts, n, out, R);
+}
+void vdo_circumsphere_float(int dim, const double* v, double* center, double* radius) {
+  circumsphere_float(dim, v, center, radius);
+}
+uint32_t vdo_priority(uint32_t vid, uint64_t seed) { return priority(vid, seed); }
+
+// ---- exact predicates (pts are (dim+1) or (dim+2) xyz triples) -----------
+int vdo_orient(int dim, const double* pts) {
+  P3 p[4];
+  for (int i = 0; i <= dim; ++i) p[i] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+  return exact_orient(dim, p);
+}
+int vdo_insphere_sos(int dim, const double* pts, const int* keys) {
+  P3 p[4], q;
+  for (int i = 0; i <= dim; ++i) p[i] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+  int k = dim + 1;
+  q = {pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]};
+  return insphere_sos(dim, p, keys, q, keys[k], nullptr, nullptr);
+}
+// exact unperturbed lifted determinant sign
+int vdo_insphere_exact(int dim, const double* pts) {
+  P3 p[4], q;
+  for (int i = 0; i <= dim; ++i) p[i] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+  int k = dim + 1;
+  q = {pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]};
+  int os[4], ds;
+  exact_lifted(dim, p, q, os, &ds);
+  return ds;
+}
+
+// ---- sequential triangulation ---------------------------------------------
+// pts: n points of `dim` doubles.  The super simplex is sized from the same
+// points (src/lib.rs:104-125).  Returns an opaque handle; *status is 0 or an
+// error code.  Duplicates are skipped (kept: smallest priority).
+void* vdo_build(int dim, const double* pts, int64_t n, uint64_t seed, int* status) {
+  Tree* t = new Tree();
+  t->dim = dim;
+  t->ns = dim + 1;
+  *status = OK;
+  if ((dim != 2 && dim != 3) || n < 1) {
+    *status = ERR_ARG;
+    return t;
+  }
+  double sv[12], R;
+  super_vertices(dim, pts, n, sv, &R);
+  for (int i = 0; i <= dim; ++i) t->pts.push_back({sv[3 * i], sv[3 * i + 1], sv[3 * i + 2]});
+  for (int64_t k = 0; k < n; ++k)
+    t->pts.push_back({pts[k * dim], pts[k * dim + 1], dim == 3 ? pts[k * dim + 2] : 0.0});
+  Simplex s0;
+  s0.alive = true;
+  for (int i = 0; i < 4; ++i) {
+    s0.v[i] = i <= dim ? i : -1;
+    s0.n[i] = -1;
+  }
+  {  // positive orientation
+    P3 q[4];
+    for (int i = 0; i <= dim; ++i) q[i] = t->pts[i];
+    int o = exact_orient(dim, q);
+    if (o == 0) {
+      *status = ERR_DEGENERATE;
+      return t;
+    }
+    if (o < 0) std::swap(s0.v[0], s0.v[1]);
+  }
+  t->s.push_back(s0);
+  // duplicate groups: keep the smallest priority
+  t->dup_of.assign(n, -1);
+  {
+    struct K {
+      double x, y, z;
+      bool operator==(const K& o) const { return x == o.x && y == o.y && z == o.z; }
+    };
+    struct H {
+      size_t operator()(const K& k) const {
+        uint64_t a, b, c;
+        memcpy(&a, &k.x, 8);
+        memcpy(&b, &k.y, 8);
+        memcpy(&c, &k.z, 8);
+        return (size_t)(a * 0x9E3779B97F4A7C15ULL ^ (b + 0x632BE59BD9B4E019ULL) * 31 ^ c);
+      }
+    };
+    std::unordered_map<K, int64_t, H> best;
+    best.reserve(n * 2);
+    for (int64_t k = 0; k < n; ++k) {
+      const P3& p = t->pts[t->ns + k];
+      K key{p.x == 0.0 ? 0.0 : p.x, p.y == 0.0 ? 0.0 : p.y, p.z == 0.0 ? 0.0 : p.z};
+      auto it = best.find(key);
+      if (it == best.end()) {
+        best.emplace(key, k);
+      } else {
+        int64_t j = it->second;
+        uint32_t pk = priority((uint32_t)(t->ns + k), seed), pj = priority((uint32_t)(t->ns + j), seed);
+        if (pk < pj) {
+          t->dup_of[j] = (int)k;
+          it->second = k;
+        } else {
+          t->dup_of[k] = (int)j;
+        }
+      }
+    }
+    // resolve chains to the final kept index
+    for (int64_t k = 0; k < n; ++k) {
+      if (t->dup_of[k] < 0) continue;
+      const P3& p = t->pts[t->ns + k];
+      K key{p.x == 0.0 ? 0.0 : p.x, p.y == 0.0 ? 0.0 : p.y, p.z == 0.0 ? 0.0 : p.z};
+      t->dup_of[k] = (int)best[key];
+    }
+  }
+  for (int64_t k = 0; k < n; ++k) {
+    if (t->dup_of[k] >= 0) continue;
+    int rc = insert_vertex(*t, (int)(t->ns + k));
+    if (rc != OK) {
+      *status = rc;
+      return t;
+    }
+  }
+  return t;
+}
+
+void vdo_free(void* h) { delete (Tree*)h; }
+
+int64_t vdo_num_duplicates(void* h) {
+  Tree* t = (Tree*)h;
+  int64_t c = 0;
+  for (int d : t->dup_of) c += d >= 0;
+  return c;
+}
+
+void vdo_stats(void* h, long long* out) {
+  Tree* t = (Tree*)h;
+  long long alive = 0;
+  for (auto& s : t->s) alive += s.alive;
+  out[0] = alive;
+  out[1] = (long long)t->s.size();
+  out[2] = t->nexact;
+  out[3] = t->nsos;
+  out[4] = t->nwalk;
+  out[5] = t->maxcav;
+  out[6] = t->maxfac;
+}
+
+// Sorted unique edge list among input points (input indices, u < v).
+int64_t vdo_edges(void* h, int64_t* uv, int64_t cap) {
+  Tree* t = (Tree*)h;
+  std::vector<uint64_t> e;
+  int nv = t->dim + 1;
+  for (auto& s : t->s) {
+    if (!s.alive) continue;
+    for (int i = 0; i < nv; ++i)
+      for (int j = i + 1; j < nv; ++j) {
+        int a = s.v[i], b = s.v[j];
+        if (a < t->ns || b < t->ns) continue;
+        a -= t->ns;
+        b -= t->ns;
+        if (a > b) std::swap(a, b);
+        e.push_back(((uint64_t)a << 32) | (uint32_t)b);
+      }
+  }
+  std::sort(e.begin(), e.end());
+  e.erase(std::unique(e.begin(), e.end()), e.end());
+  if (uv) {
+    int64_t m = std::min<int64_t>(cap, (int64_t)e.size());
+    for (int64_t i = 0; i < m; ++i) {
+      uv[2 * i] = (int64_t)(e[i] >> 32);
+      uv[2 * i + 1] = (int64_t)(e[i] & 0xffffffffu);
+    }
+  }
+  return (int64_t)e.size();
+}
+
+// Vertex coordinates (super first) and alive simplices in the handle's own
+// numbering, for the validator.
+int64_t vdo_num_vertices(void* h) { return (int64_t)((Tree*)h)->pts.size(); }
+void vdo_vertices(void* h, double* xyz) {
+  Tree* t = (Tree*)h;
+  for (size_t i = 0; i < t->pts.size(); ++i) {
+    xyz[3 * i] = t->pts[i].x;
+    xyz[3 * i + 1] = t->pts[i].y;
+    xyz[3 * i + 2] = t->pts[i].z;
+  }
+}
+
+// ---- validator for any triangulation -------------------------------------
+// verts: nvert xyz triples (vertex id = index, super vertices first).
+// simp: ns rows of 4 vertex ids (2D: 3 used), nbr: ns rows of 4 neighbour
+// simplex indices (row-local, -1 = hull).  out[0..7]:
+//  0 non-positive simplices, 1 asymmetric adjacencies, 2 facets whose
+//  opposite vertex is strictly inside (exact, unperturbed), 3 facets failing
+//  the perturbed test, 4 hull facets, 5 facets checked, 6 vertices missing
+//  from every simplex (among `expect_vertices` first ids), 7 exact calls
+void vdo_validate(int dim, const double* verts, int64_t nvert, const int32_t* simp,
+                  const int32_t* nbr, int64_t ns, int64_t expect_vertices, long long* out) {
+  for (int i = 0; i < 8; ++i) out[i] = 0;
+  int nv = dim + 1;
+  auto P = [&](int v) { return P3{verts[3 * v], verts[3 * v + 1], verts[3 * v + 2]}; };
+  std::vector<char> seen(nvert, 0);
+  long long nex = 0;
+  for (int64_t s = 0; s < ns; ++s) {
+    const int32_t* v = simp + 4 * s;
+    P3 q[4];
+    for (int i = 0; i < nv; ++i) {
+      q[i] = P(v[i]);
+      seen[v[i]] = 1;
+    }
+    if (orient(dim, q, &nex) <= 0) out[0]++;
+    for (int f = 0; f < nv; ++f) {
+      int o = nbr[4 * s + f];
+      if (o < 0) {
+        out[4]++;
+        continue;
+      }
+      // neighbour must point back and share the facet
+      const int32_t* w = simp + 4 * o;
+      int back = -1;
+      for (int g = 0; g < nv; ++g)
+        if (nbr[4 * o + g] == s) back = g;
+      bool ok = back >= 0;
+      if (ok) {
+        for (int i = 0; i < nv; ++i) {
+          if (i == f) continue;
+          bool found = false;
+          for (int g = 0; g < nv; ++g)
+            if (g != back && w[g] == v[i]) found = true;
+          ok = ok && found;
+        }
+      }
+      if (!ok) {
+        out[1]++;
+        continue;
+      }
+      if (o < s) continue;  // each interior facet once
+      out[5]++;
+      int opp = w[back];
+      P3 e = P(opp);
+      int ds;
+      int os[4];
+      exact_lifted(dim, q, e, os, &ds);
+      ++nex;
+      if (ds > 0) out[2]++;
+      int key[4];
+      for (int i = 0; i < nv; ++i) key[i] = v[i];
+      if (insphere_sos(dim, q, key, e, opp, nullptr, nullptr) > 0) out[3]++;
+    }
+  }
+  for (int64_t i = 0; i < expect_vertices && i < nvert; ++i)
+    if (!seen[i]) out[6]++;
+  out[7] = nex;
+}
+
+// Export alive simplices of an oracle handle (same layout as vdo_validate).
+int64_t vdo_simplices(void* h, int32_t* simp, int32_t* nbr) {
+  Tree* t = (Tree*)h;
+  std::vector<int> remap(t->s.size(), -1);
+  int64_t k = 0;
+  for (size_t i = 0; i < t->s.size(); ++i)
+    if (t->s[i].alive) remap[i] = (int)k++;
+  if (simp) {
+    int64_t r = 0;
+    for (size_t i = 0; i < t->s.size(); ++i) {
+      if (!t->s[i].alive) continue;
+      for (int j = 0; j < 4; ++j) {
+        simp[4 * r + j] = t->s[i].v[j];
+        int nb = t->s[i].n[j];
+        nbr[4 * r + j] = (j <= t->dim && nb >= 0) ? remap[nb] : -1;
+      }
+      ++r;
+    }
+  }
+  return k;
+}
+
+int vdo_status(void* h) { return ((Tree*)h)->status; }
+
+}  // extern "C"

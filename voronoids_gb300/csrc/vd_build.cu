@@ -1,0 +1,1143 @@
+// Round-parallel Bowyer-Watson insertion on one GPU.
+//
+// One round replaces one `add_points_to_tree` batch of the reference
+// (src/delaunay_tree.rs:336-386; queue + placement in src/scheduler.rs:6-55):
+//
+//   k_pick      every simplex that holds uninserted points nominates the one
+//               with the lowest priority (votes were cast by the previous
+//               k_relocate); a nominee claims its simplex and the face
+//               neighbours (thinning) so that only locally lowest nominees
+//               pay for a cavity search.
+//   k_cavity    one warp per surviving nominee: breadth-first search of the
+//               conflict region from the simplex that contains it (`locate` +
+//               `find_all_neighbors`, src/delaunay_tree.rs:33-75) with exact
+//               perturbed in-sphere tests, collection of the boundary facets
+//               (`get_new_simplices`, :77-123), then atomicMin claims with the
+//               candidate's priority on the cavity (claim_c) and on every outer
+//               neighbour whose face it will rewrite (claim_n).
+//   k_check /   resolution passes, one warp per candidate: the independence
+//   k_reclaim   test (see k_check), then winners write the star (killed slots
+//               first, then fresh slots), link it internally by matching ridges
+//               (`pair_simplices`, :674-695) and repoint the outer faces
+//               (`insert_points_parallel`, :213-334).  Winners are pairwise
+//               independent: no winner's point lies in another winner's new
+//               simplices, so a round equals some sequential insertion order.
+//   k_relocate  one thread per uninserted point: points whose simplex was
+//               removed walk inside the new star (faces through the new vertex
+//               only) to the simplex that contains them; every point then votes
+//               for the next round; survivors are compacted.
+//
+// A point is always located in a simplex that contains it, and a closed
+// simplex meets its circumsphere only in its vertices, so the containing
+// simplex is in conflict unless the point duplicates one of its vertices,
+// which k_cavity detects and drops.
+#include <cuda_runtime.h>
+
+#include "vd_common.cuh"
+
+namespace vd {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <int D>
+struct Cap;
+template <>
+struct Cap<3> {
+  static constexpr int MAXC = 128, MAXF = 192, HS = 256;
+};
+template <>
+struct Cap<2> {
+  static constexpr int MAXC = 64, MAXF = 96, HS = 128;
+};
+
+__device__ __forceinline__ int get4(const int4& a, int i) {
+  return i == 0 ? a.x : (i == 1 ? a.y : (i == 2 ? a.z : a.w));
+}
+__device__ __forceinline__ int4 set4(int4 a, int i, int v) {
+  if (i == 0) a.x = v;
+  else if (i == 1) a.y = v;
+  else if (i == 2) a.z = v;
+  else a.w = v;
+  return a;
+}
+__device__ __forceinline__ void load_simplex(const DevTree& T, int s, int4& v, int4& n) {
+  if (bad_simp(T, s)) {
+    set_error(T.ctr, E_INTERNAL);
+    s = 0;
+  }
+  const int4* p = reinterpret_cast<const int4*>(T.simp + s);
+  v = p[0];
+  n = p[1];
+}
+__device__ __forceinline__ void store_simplex(const DevTree& T, int s, int4 v, int4 n) {
+  if (bad_simp(T, s)) {
+    set_error(T.ctr, E_INTERNAL);
+    return;
+  }
+  int4* p = reinterpret_cast<int4*>(T.simp + s);
+  p[0] = v;
+  p[1] = n;
+}
+__device__ __forceinline__ vdp::VPt load_pt(const DevTree& T, int v) {
+  if (bad_vert(T, v)) {
+    set_error(T.ctr, E_INTERNAL);
+    v = 0;
+  }
+  const double4_32a a = reinterpret_cast<const double4_32a*>(T.pts)[v];
+  return vdp::VPt{a.x, a.y, a.z, a.w};
+}
+
+__device__ __forceinline__ vdp::FPt load_fpt(const DevTree& T, int v) {
+  if (bad_vert(T, v)) {
+    set_error(T.ctr, E_INTERNAL);
+    v = 0;
+  }
+  const float4* p = reinterpret_cast<const float4*>(T.ptf + v);
+  const float4 h = p[0], l = p[1];
+  return vdp::FPt{h.x, h.y, h.z, h.w, l.x, l.y, l.z, l.w};
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+  return v;
+}
+__device__ void flush_tally(Counters* c, const vdp::Tally& t, unsigned long long tests,
+                            unsigned long long walk) {
+  unsigned long long a = warp_sum(t.f32), b = warp_sum(t.f64), e = warp_sum(t.exact),
+                     s = warp_sum(t.sos), x = warp_sum(tests), w = warp_sum(walk);
+  if ((threadIdx.x & 31) == 0) {
+    if (a) atomicAdd(&c->tally[0], a);
+    if (b) atomicAdd(&c->tally[1], b);
+    if (e) atomicAdd(&c->tally[2], e);
+    if (s) atomicAdd(&c->tally[3], s);
+    if (x) atomicAdd(&c->cavity_tests, x);
+    if (w) atomicAdd(&c->walk, w);
+  }
+}
+
+// Warp-aggregated atomicMin of `val` into vote[loc] for all lanes with
+// `active`; lanes that share a location are combined first.
+__device__ __forceinline__ void vote_min(unsigned long long* vote, bool active, int loc,
+                                         unsigned long long val) {
+  unsigned am = __ballot_sync(FULL, active);
+  if (!active) return;
+  unsigned grp = __match_any_sync(am, loc);
+  unsigned long long m = val;
+  // min over the group: each lane pulls from every other member
+  for (unsigned g = grp; g; g &= g - 1) {
+    int src = __ffs(g) - 1;
+    unsigned long long o = __shfl_sync(grp, val, src);
+    m = o < m ? o : m;
+  }
+  if ((threadIdx.x & 31) == __ffs(grp) - 1) atomicMin(vote + loc, m);
+}
+
+// Warp-aggregated append; returns the slot for lanes with `flag`.
+__device__ __forceinline__ int warp_append(int* counter, bool flag) {
+  unsigned m = __ballot_sync(FULL, flag);
+  if (!m) return -1;
+  int lane = threadIdx.x & 31, leader = __ffs(m) - 1, base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(FULL, base, leader);
+  return flag ? base + __popc(m & ((1u << lane) - 1)) : -1;
+}
+
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_upload(DevTree T, const double* xyz, long long n, int base, int4 sup) {
+  constexpr int NV = D + 1;
+  const double lo = 7.006492321624085e-46;  // 2^-150
+  const double hi = 1.4272476927059599e45;  // 2^150
+  vdp::Tally tl = {0, 0, 0, 0};
+  int perr = 0;
+  vdp::VPt sv[NV];
+  for (int j = 0; j < NV; ++j) sv[j] = load_pt(T, get4(sup, j));
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double c[3] = {xyz[i * D], xyz[i * D + 1], D == 3 ? xyz[i * D + 2] : 0.0};
+    for (int k = 0; k < 3; ++k) {
+      double a = fabs(c[k]);
+      if (!(a <= 1.7976931348623157e308)) set_error(T.ctr, E_NONFINITE);
+      else if (a != 0.0 && (a < lo || a > hi)) set_error(T.ctr, E_RANGE);
+    }
+    vdp::VPt p{c[0], c[1], c[2], 0.0};
+    reinterpret_cast<double4_32a*>(T.pts)[base + i] = make_double4_32a(c[0], c[1], c[2], 0.0);
+    T.ptf[base + i] = vdp::split_point(c[0], c[1], c[2]);
+    if (vdp::exit_face<D, true>(sv, p, (1u << NV) - 1, tl, perr) >= 0) set_error(T.ctr, E_OUTSIDE);
+  }
+  if (perr) set_error(T.ctr, E_PRECISION);
+}
+
+// Multi-level grid of location hints.  Level l splits the sizing box
+// (centre +- bounding radius) into 2^l cells per axis; each cell keeps the
+// slot of a simplex created near it (written by every winner, races are
+// harmless: any live simplex is a valid walk start, a near one is a short
+// walk).
+template <int D>
+__device__ __forceinline__ int hint_index(const DevTree& T, const vdp::VPt& p, int level) {
+  const int side = 1 << level;
+  const double c[3] = {p.x, p.y, p.z};
+  int idx = 0;
+  for (int k = D - 1; k >= 0; --k) {
+    double u = (c[k] - T.gorg[k]) * T.gscale;
+    int i = (int)(u * side);
+    i = i < 0 ? 0 : (i >= side ? side - 1 : i);
+    idx = idx * side + i;
+  }
+  const int off = D == 3 ? ((1 << (3 * level)) - 1) / 7 : ((1 << (2 * level)) - 1) / 3;
+  return off + idx;
+}
+
+template <int D>
+__device__ __forceinline__ void write_hints(const DevTree& T, const vdp::VPt& q, int slot) {
+  for (int l = 0; l <= T.hint_levels; ++l) T.hint[hint_index<D>(T, q, l)] = slot;
+}
+
+// Priority-prefix histogram: prefix k holds the points with
+// thr[k-1] <= priority < thr[k].
+struct Thresholds {
+  unsigned long long t[kMaxPrefixes];
+  int n;
+};
+
+__global__ void k_prefix_hist(long long n, int base, unsigned long long seed, Thresholds th, int* counts) {
+  __shared__ int sh[kMaxPrefixes];
+  for (int k = threadIdx.x; k < kMaxPrefixes; k += blockDim.x) sh[k] = 0;
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long pr = priority((uint32_t)(base + i), seed);
+    int k = 0;
+    while (k < th.n - 1 && pr >= th.t[k]) ++k;
+    atomicAdd(&sh[k], 1);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < th.n; k += blockDim.x)
+    if (sh[k]) atomicAdd(counts + k, sh[k]);
+}
+
+// Activates the points of one priority prefix: each walks from the finest
+// available grid hint to the simplex that contains it (visibility walk,
+// exact orientation), joins the active list and votes for this round.
+template <int D>
+__global__ void k_activate(DevTree T, long long n, int base, unsigned long long seed,
+                           unsigned long long lo, unsigned long long hi, int round) {
+  constexpr int NV = D + 1;
+  const int par = round & 1;
+  const unsigned long long ep = epoch(round);
+  vdp::Tally tl = {0, 0, 0, 0};
+  int perr = 0;
+  unsigned long long walk = 0;
+  const int cap = 1 << 16;
+  for (long long b = blockIdx.x * (long long)blockDim.x; b < n; b += (long long)gridDim.x * blockDim.x) {
+    const long long i = b + threadIdx.x;
+    bool act = false;
+    int cur = 0;
+    unsigned pr = 0;
+    int vid = 0;
+    if (i < n) {
+      vid = base + (int)i;
+      pr = priority((uint32_t)vid, seed);
+      act = pr >= lo && pr < hi;
+    }
+    if (act) {
+      const vdp::VPt p = load_pt(T, vid);
+      cur = -1;
+      for (int l = T.hint_levels; l >= 0 && cur < 0; --l) cur = T.hint[hint_index<D>(T, p, l)];
+      if (cur < 0) cur = 0;  // no insertion yet: the super simplex
+      int4 v, nn;
+      load_simplex(T, cur, v, nn);
+      for (int k = 0; k < 64 && v.x < 0; ++k) {  // dead slot: follow it into its star
+        cur = nn.x >> 2;
+        if (nn.x < 0 || bad_simp(T, cur)) {
+          set_error(T.ctr, E_INTERNAL);
+          cur = 0;
+        }
+        load_simplex(T, cur, v, nn);
+      }
+      const vdp::FPt fp = load_fpt(T, vid);
+      int step = 0;
+      for (; step < cap; ++step) {
+        vdp::FPt fv[NV];
+        for (int j = 0; j < NV; ++j) fv[j] = load_fpt(T, get4(v, j));
+        auto load64 = [&](vdp::VPt* v64, vdp::VPt& p64) {
+          for (int j = 0; j < NV; ++j) v64[j] = load_pt(T, get4(v, j));
+          p64 = p;
+        };
+        const int f = vdp::exit_face_hl<D>(fv, fp, (1u << NV) - 1, tl, perr, load64);
+        if (f < 0) break;
+        const int code = get4(nn, f);
+        if (code < 0 || bad_simp(T, code >> 2)) {
+          set_error(T.ctr, code < 0 ? E_OUTSIDE : E_INTERNAL);
+          break;
+        }
+        cur = code >> 2;
+        load_simplex(T, cur, v, nn);
+        ++walk;
+      }
+      if (step == cap) set_error(T.ctr, E_WALK);
+    }
+    vote_min(T.vote, act, cur, ep | pr);
+    const int k = warp_append(&T.ctr->nact[par], act);
+    if (act) T.act[par][k] = make_int4(vid, cur, (int)pr, 0);
+  }
+  if (perr) set_error(T.ctr, E_PRECISION);
+  flush_tally(T.ctr, tl, 0, walk);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_pick(DevTree T, int round) {
+  const int par = round & 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) T.ctr->nact[par ^ 1] = 0;
+  const int n = T.ctr->nact[par];
+  const unsigned long long ep = epoch(round);
+  unsigned long long ncand = 0;
+  for (int b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+    int i = b + threadIdx.x;
+    bool is = false;
+    int4 e = make_int4(-1, 0, 0, 0);
+    if (i < n) {
+      e = T.act[par][i];
+      is = e.x >= 0 && T.vote[e.y] == (ep | (unsigned)e.z);
+    }
+    int k = warp_append(&T.ctr->ncand, is);
+    if (is) {
+      ++ncand;
+      if (k < T.cap_cand) T.cand[k] = make_int4(e.x, e.y, e.z, i);
+      // thinning claim: the home simplex and its face neighbours
+      const unsigned long long key = ep | (unsigned)e.z;
+      int4 v, nn;
+      load_simplex(T, e.y, v, nn);
+      atomicMin(T.thin + e.y, key);
+      const int nb[4] = {nn.x, nn.y, nn.z, nn.w};
+      for (int f = 0; f < 4; ++f)
+        if (nb[f] >= 0 && !bad_simp(T, nb[f] >> 2)) atomicMin(T.thin + (nb[f] >> 2), key);
+    }
+  }
+  ncand = warp_sum(ncand);
+  if ((threadIdx.x & 31) == 0 && ncand) atomicAdd(&T.ctr->candidates, ncand);
+}
+
+// Storage of one cavity search: shared memory for the common case, a
+// reserved, 16-byte aligned stretch of the round's cavity pool when that
+// overflows.  Generic pointers let the same code run on both.
+struct CavStore {
+  int* cav;     // simplex ids of the conflict region
+  int4* cv;     // their vertex ids
+  int4* cn;     // their neighbour codes
+  int* hk;      // open-addressing set of cavity ids (hs slots, power of two)
+  int* fr;      // boundary facets, 6 ints each: new simplex vertices (4), outer code, (k << 2) | face
+  int maxc, maxf, hs;
+};
+
+// Spill stretch layout (ints): cavity ids | facet records | cv | cn | id set |
+// ridge table (keys 2 ints + partners 2 ints per slot).  The search uses the
+// first five parts, the commit of a large star the facets and the ridge table.
+constexpr int kBigC = 8192, kBigF = 12288, kBigH = 32768, kBigR = 65536;
+// Fresh simplex slots a warp takes at a time in k_check.
+constexpr int kSlotChunk = 32;
+constexpr int kOffF = kBigC;
+constexpr int kOffCV = kOffF + 6 * kBigF;
+constexpr int kOffCN = kOffCV + 4 * kBigC;
+constexpr int kOffH = kOffCN + 4 * kBigC;
+constexpr int kOffR = kOffH + kBigH;
+constexpr int kBigInts = kOffR + 4 * kBigR;  // multiple of 4
+
+__device__ bool hset_insert(int* hk, int hs, int key) {
+  unsigned h = ((unsigned)key * 2654435761u) & (hs - 1);
+  for (int probe = 0; probe < hs; ++probe) {
+    int old = atomicCAS(&hk[h], -1, key);
+    if (old == -1) return true;
+    if (old == key) return false;
+    h = (h + 1) & (hs - 1);
+  }
+  return false;
+}
+__device__ bool hset_find(const int* hk, int hs, int key) {
+  unsigned h = ((unsigned)key * 2654435761u) & (hs - 1);
+  for (int probe = 0; probe < hs; ++probe) {
+    int k = *((volatile const int*)&hk[h]);
+    if (k == key) return true;
+    if (k == -1) return false;
+    h = (h + 1) & (hs - 1);
+  }
+  return false;
+}
+
+struct WarpCtl {
+  int ncav, nfac, flags, pad;
+};
+
+// Breadth-first search of the conflict region of candidate q from the
+// simplex that contains it; all 32 lanes of the warp call this.  Returns
+// with ctl.flags != 0 if a capacity was exceeded.
+template <int D>
+__device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl, int lane, int start,
+                              int4 v0, int4 n0, int qv, const vdp::VPt& q, const vdp::FPt& fq,
+                              vdp::Tally& tl, int& perr, unsigned long long& ntests) {
+  constexpr int NV = D + 1;
+  for (int i = lane; i < S.hs; i += 32) S.hk[i] = -1;
+  if (lane == 0) {
+    ctl.ncav = 1;
+    ctl.nfac = 0;
+    ctl.flags = 0;
+    S.cav[0] = start;
+    S.cv[0] = v0;
+    S.cn[0] = n0;
+  }
+  __syncwarp();
+  if (lane == 0) hset_insert(S.hk, S.hs, start);
+  __syncwarp();
+  int head = 0;
+  while (true) {
+    const int hi = min(*(volatile int*)&ctl.ncav, S.maxc);
+    if (*(volatile int*)&ctl.flags || head >= hi) break;
+    const int items = (hi - head) * NV;
+    for (int it = lane; it < items; it += 32) {
+      const int k = head + it / NV, f = it - (it / NV) * NV;
+      const int code = get4(S.cn[k], f);
+      bool facet = code < 0;
+      if (!facet && bad_simp(T, code >> 2)) {
+        set_error(T.ctr, E_INTERNAL);
+        continue;
+      }
+      if (!facet) {
+        const int nb = code >> 2;
+        if (!hset_find(S.hk, S.hs, nb)) {
+          int4 vv, nn;
+          load_simplex(T, nb, vv, nn);
+          vdp::FPt fv[NV];
+          int kv[NV];
+          for (int j = 0; j < NV; ++j) {
+            kv[j] = get4(vv, j);
+            fv[j] = load_fpt(T, kv[j]);
+          }
+          ++ntests;
+          auto load64 = [&](vdp::VPt* v64, vdp::VPt& q64) {
+            for (int j = 0; j < NV; ++j) v64[j] = load_pt(T, kv[j]);
+            q64 = q;
+          };
+          if (vdp::in_conflict_hl<D>(fv, kv, fq, qv, tl, perr, load64)) {
+            if (hset_insert(S.hk, S.hs, nb)) {
+              int s = atomicAdd(&ctl.ncav, 1);
+              if (s < S.maxc) {
+                S.cav[s] = nb;
+                S.cv[s] = vv;
+                S.cn[s] = nn;
+              } else {
+                atomicOr(&ctl.flags, 1);
+              }
+            }
+          } else {
+            facet = true;
+          }
+        }
+      }
+      if (facet) {
+        int s = atomicAdd(&ctl.nfac, 1);
+        if (s < S.maxf) {
+          const int4 nv4 = set4(S.cv[k], f, qv);
+          int* r = S.fr + 6 * s;
+          r[0] = nv4.x;
+          r[1] = nv4.y;
+          r[2] = nv4.z;
+          r[3] = nv4.w;
+          r[4] = code;
+          r[5] = (k << 2) | f;
+        } else {
+          atomicOr(&ctl.flags, 2);
+        }
+      }
+    }
+    __syncwarp();
+    head = hi;
+  }
+  __syncwarp();
+}
+
+template <int D>
+struct WarpCav {
+  WarpCtl ctl;
+  int cav[Cap<D>::MAXC];
+  int4 cv[Cap<D>::MAXC];
+  int4 cn[Cap<D>::MAXC];
+  int hkey[Cap<D>::HS];
+  int fr[6 * Cap<D>::MAXF];
+};
+
+// Claims of a candidate for one resolution pass: its cavity in claim_c, every
+// outer neighbour in claim_n.  P = cavity ids, F = facet records.
+__device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int ncav, const int* F,
+                                             int nfac, unsigned long long key, int lane) {
+  for (int i = lane; i < ncav; i += 32) atomicMin(T.claim_c + P[i], key);
+  for (int j = lane; j < nfac; j += 32) {
+    const int o = F[6 * j + 4];
+    if (o >= 0 && !bad_simp(T, o >> 2)) atomicMin(T.claim_n + (o >> 2), key);
+  }
+}
+
+// Thinning test of one nominee (one thread): it must hold the thinning claim
+// on its simplex and on every face neighbour; with `thin` >= 2 no lower
+// nominee may claim a simplex two faces away either.
+template <int D>
+__device__ bool thin_lost1(const DevTree& T, int home, int4 n0, unsigned long long key, int thin) {
+  constexpr int NV = D + 1;
+  if (T.thin[home] != key) return true;
+  for (int f = 0; f < NV; ++f) {
+    const int nb = get4(n0, f);
+    if (nb < 0 || bad_simp(T, nb >> 2)) continue;
+    if (T.thin[nb >> 2] != key) return true;
+  }
+  if (thin >= 2) {
+    for (int f = 0; f < NV; ++f) {
+      const int nb = get4(n0, f);
+      if (nb < 0 || bad_simp(T, nb >> 2)) continue;
+      int4 v2, n2;
+      load_simplex(T, nb >> 2, v2, n2);
+      for (int g = 0; g < NV; ++g) {
+        const int x = get4(n2, g);
+        if (x >= 0 && !bad_simp(T, x >> 2) && T.thin[x >> 2] < key) return true;
+      }
+    }
+  }
+  return false;
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_cavity(DevTree T, int round, int thin) {
+  constexpr int NV = D + 1, MAXC = Cap<D>::MAXC, MAXF = Cap<D>::MAXF, HS = Cap<D>::HS;
+  __shared__ WarpCav<D> smem[4];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WarpCav<D>& W = smem[wib];
+  const int nc = min(T.ctr->ncand, T.cap_cand);
+  const unsigned long long ep = epoch(round);
+  const unsigned long long pe = pass_epoch(round, 0);
+  const int par = round & 1;
+  vdp::Tally tl = {0, 0, 0, 0};
+  int perr = 0;
+  unsigned long long ntests = 0, nsearched = 0, nspill = 0;
+  int mcav = 0, mfac = 0;
+  // pool space is taken in per-warp chunks (one atomic per chunk, not per
+  // candidate); what a warp leaves unused is dropped with the round's pool
+  const int pchunk = max(256, min(8192, T.cap_pool / (gridDim.x * 16)));
+  int pbase = 0, pleft = 0;
+  const CavStore fast{W.cav, W.cv, W.cn, W.hkey, W.fr, MAXC, MAXF, HS};
+  // Warps take strips of 32 nominees: duplicate and thinning tests run one
+  // nominee per lane, then the warp searches the survivors one by one.
+  for (int base = (blockIdx.x * 4 + wib) * 32; base < nc; base += gridDim.x * 4 * 32) {
+    const int cl = base + lane;
+    bool survive = false;
+    if (cl < nc) {
+      const int4 e = T.cand[cl];
+      int4 v, n;
+      load_simplex(T, e.y, v, n);
+      const vdp::VPt q = load_pt(T, e.x);
+      int dup = -1;
+      for (int j = 0; j < NV; ++j) {
+        const int vid = get4(v, j);
+        if (vdp::same_point(load_pt(T, vid), q)) dup = vid;
+      }
+      if (dup >= 0) {
+        T.act[par][e.w].x = -1;
+        const int k = atomicAdd(&T.ctr->ndup, 1);
+        if (k < T.cap_dups) T.dups[k] = make_int2(e.x, dup);
+        T.cinfo[cl] = make_int4(0, 0, 0, ST_DUP);
+      } else if (thin_lost1<D>(T, e.y, n, ep | (unsigned)e.z, thin)) {
+        T.cinfo[cl] = make_int4(0, 0, 0, ST_LOST);
+      } else {
+        survive = true;
+      }
+    }
+    unsigned todo = __ballot_sync(FULL, survive);
+    while (todo) {
+    const int src = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const int c = base + src;
+    const int4 cd = T.cand[c];
+    const vdp::VPt q = load_pt(T, cd.x);
+    const vdp::FPt fq = load_fpt(T, cd.x);
+    int4 v0, n0;
+    load_simplex(T, cd.y, v0, n0);
+    if (lane == 0) ++nsearched;
+    const unsigned long long key = pe | (unsigned)cd.z;
+    cavity_search<D>(T, fast, W.ctl, lane, cd.y, v0, n0, cd.x, q, fq, tl, perr, ntests);
+    int ncav = min(W.ctl.ncav, MAXC), nfac = min(W.ctl.nfac, MAXF);
+    int off = 0;
+    if (W.ctl.flags) {
+      // spill: redo the search with its lists in a reserved pool stretch
+      if (lane == 0) {
+        ++nspill;
+        off = atomicAdd(&T.ctr->pool_used, kBigInts + 4);
+      }
+      off = (__shfl_sync(FULL, off, 0) + 3) & ~3;  // int4 alignment of cv / cn
+      if (off + kBigInts > T.cap_pool) {
+        if (lane == 0) {
+          T.cinfo[c] = make_int4(0, 0, 0, ST_POOL);
+          atomicAdd(&T.ctr->pool_overflow, 1);
+        }
+        __syncwarp();
+        continue;
+      }
+      int* P = T.pool + off;
+      const CavStore big{P, reinterpret_cast<int4*>(P + kOffCV), reinterpret_cast<int4*>(P + kOffCN),
+                         P + kOffH, P + kOffF, kBigC, kBigF, kBigH};
+      cavity_search<D>(T, big, W.ctl, lane, cd.y, v0, n0, cd.x, q, fq, tl, perr, ntests);
+      if (W.ctl.flags) {
+        if (lane == 0) {
+          T.cinfo[c] = make_int4(W.ctl.ncav, W.ctl.nfac, 0, ST_OVERFLOW);
+          atomicAdd(&T.ctr->overflow, 1);
+        }
+        __syncwarp();
+        continue;
+      }
+      ncav = W.ctl.ncav;
+      nfac = W.ctl.nfac;
+      // the facets stay at P + kOffF; cinfo.y carries the flag (see below)
+      claim_region(T, P, ncav, P + kOffF, nfac, key, lane);
+      if (lane == 0) T.cinfo[c] = make_int4(ncav, nfac | (1 << 30), off, ST_OK);
+      mcav = max(mcav, ncav);
+      mfac = max(mfac, nfac);
+      __syncwarp();
+      continue;
+    }
+    const int need = ncav + nfac * 6;
+    if (need > pleft) {
+      const int take = max(need, pchunk);
+      if (lane == 0) pbase = atomicAdd(&T.ctr->pool_used, take);
+      pbase = __shfl_sync(FULL, pbase, 0);
+      pleft = take;
+      if (pbase + take > T.cap_pool) pleft = 0;
+    }
+    if (need > pleft) {
+      if (lane == 0) {
+        T.cinfo[c] = make_int4(ncav, nfac, 0, ST_POOL);
+        atomicAdd(&T.ctr->pool_overflow, 1);
+      }
+      __syncwarp();
+      continue;
+    }
+    off = pbase;
+    pbase += need;
+    pleft -= need;
+    int* P = T.pool + off;
+    for (int i = lane; i < ncav; i += 32) P[i] = W.cav[i];
+    int* F = P + ncav;
+    for (int x = lane; x < 6 * nfac; x += 32) F[x] = W.fr[x];
+    claim_region(T, W.cav, ncav, W.fr, nfac, key, lane);
+    if (lane == 0) T.cinfo[c] = make_int4(ncav, nfac, off, ST_OK);
+    mcav = max(mcav, ncav);
+    mfac = max(mfac, nfac);
+    __syncwarp();
+    }
+  }
+  if (perr) set_error(T.ctr, E_PRECISION);
+  flush_tally(T.ctr, tl, ntests, 0);
+  nsearched = warp_sum(nsearched);
+  nspill = warp_sum(nspill);
+  if (lane == 0) {
+    if (nsearched) atomicAdd(&T.ctr->searched, nsearched);
+    if (nspill) atomicAdd(&T.ctr->spilled, nspill);
+    if (mcav) atomicMax(&T.ctr->max_cav, mcav);
+    if (mfac) atomicMax(&T.ctr->max_fac, mfac);
+  }
+}
+
+// Pool layout of a searched candidate: cavity ids at P, facet records at
+// P + ncav, or at P + kOffF for a spilled (large) search, flagged by bit 30
+// of cinfo.y.
+__device__ __forceinline__ void cand_lists(const DevTree& T, const int4& info, int*& P, int*& F, int& ncav,
+                                           int& nfac, bool& big) {
+  P = T.pool + info.z;
+  ncav = info.x;
+  big = (info.y >> 30) & 1;
+  nfac = info.y & ((1 << 30) - 1);
+  F = big ? P + kOffF : P + ncav;
+}
+
+template <int D>
+struct WarpCommit {
+  int fr[6 * Cap<D>::MAXF];
+  int id[Cap<D>::MAXF];
+  int first[Cap<D>::MAXC];     // first facet index of each cavity simplex
+  int freeslot[Cap<D>::MAXC];  // cavity slots without an own facet
+};
+
+__device__ __forceinline__ bool has4(const int* a, int x) {
+  return a[0] == x || a[1] == x || a[2] == x || a[3] == x;
+}
+
+// Ridge of face g of new simplex r (vertices r[0..3], new vertex at qf): the
+// vertices other than r[g] and the new vertex, smaller first (2D: one vertex).
+template <int D>
+__device__ __forceinline__ void ridge_of(const int* r, int g, int qf, int& r0, int& r1) {
+  r0 = -1;
+  r1 = -1;
+  for (int i = 0; i < D + 1; ++i) {
+    if (i == g || i == qf) continue;
+    if (r0 < 0) r0 = r[i];
+    else r1 = r[i];
+  }
+  if (D == 3 && r1 < r0) {
+    const int t = r0;
+    r0 = r1;
+    r1 = t;
+  }
+}
+
+// Writes one new simplex and repoints its outer neighbour.
+__device__ __forceinline__ void emit_simplex(const DevTree& T, const int* r, int myid, int4 nn, int round) {
+  const int4 v = make_int4(r[0], r[1], r[2], r[3]);
+  const int qf = r[5] & 3, o = r[4];
+  store_simplex(T, myid, v, nn);
+  if (o >= 0 && !bad_simp(T, o >> 2)) {
+    reinterpret_cast<int*>(T.simp + (o >> 2))[4 + (o & 3)] = (myid << 2) | qf;
+    T.touched[o >> 2] = round;
+  }
+}
+
+// Star of one winner, small case: ridge partners found by scanning the facet
+// records (shared memory, at most Cap::MAXF of them).
+template <int D>
+__device__ void write_star(const DevTree& T, const int* FR, const int* ID, int nfac, int qv, int round,
+                           int lane) {
+  constexpr int NV = D + 1;
+  for (int j = lane; j < nfac; j += 32) {
+    const int* r = FR + 6 * j;
+    const int qf = r[5] & 3;
+    int4 nn = make_int4(-1, -1, -1, -1);
+    nn = set4(nn, qf, r[4]);
+    for (int g = 0; g < NV; ++g) {
+      if (g == qf) continue;
+      int r0, r1;
+      ridge_of<D>(r, g, qf, r0, r1);
+      int found = -1, pos = -1;
+      for (int m = 0; m < nfac; ++m) {
+        if (m == j) continue;
+        const int* w = FR + 6 * m;
+        if (!has4(w, r0)) continue;
+        if (D == 3 && !has4(w, r1)) continue;
+        found = m;
+        for (int i = 0; i < NV; ++i) {
+          const int x = w[i];
+          if (x != qv && x != r0 && x != r1) pos = i;
+        }
+        break;
+      }
+      if (found < 0 || pos < 0) {
+        set_error(T.ctr, E_INTERNAL);
+        continue;
+      }
+      nn = set4(nn, g, (ID[found] << 2) | pos);
+    }
+    emit_simplex(T, r, ID[j], nn, round);
+  }
+}
+
+// Star of one winner, large case: every (facet, face) inserts its ridge into
+// an open-addressing table (two halves per ridge), then reads its partner.
+template <int D>
+__device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, int nfac, int round,
+                               int* R, int lane) {
+  constexpr int NV = D + 1;
+  const unsigned mask = kBigR - 1;
+  for (int i = lane; i < 4 * kBigR; i += 32) R[i] = -1;
+  __syncwarp();
+  // R[4h] = r0, R[4h+1] = r1 (key), R[4h+2], R[4h+3] = the two half-ridges
+  for (int it = lane; it < nfac * NV; it += 32) {
+    const int j = it / NV, g = it - j * NV;
+    const int* r = FR + 6 * j;
+    const int qf = r[5] & 3;
+    if (g == qf) continue;
+    int r0, r1;
+    ridge_of<D>(r, g, qf, r0, r1);
+    unsigned h = ((unsigned)r0 * 2654435761u ^ (unsigned)(r1 + 1) * 40503u) & mask;
+    for (int probe = 0; probe < kBigR; ++probe, h = (h + 1) & mask) {
+      const int old = atomicCAS(&R[4 * h], -1, r0);
+      if (old == -1 || old == r0) {
+        // r0 matches or was just written: settle the second key word
+        const int o1 = atomicCAS(&R[4 * h + 1], -1, r1);
+        if (o1 == -1 || o1 == r1) {
+          const int side = atomicCAS(&R[4 * h + 2], -1, (j << 2) | g) == -1 ? 2 : 3;
+          if (side == 3) R[4 * h + 3] = (j << 2) | g;
+          break;
+        }
+      }
+    }
+  }
+  __syncwarp();
+  for (int j = lane; j < nfac; j += 32) {
+    const int* r = FR + 6 * j;
+    const int qf = r[5] & 3;
+    int4 nn = make_int4(-1, -1, -1, -1);
+    nn = set4(nn, qf, r[4]);
+    for (int g = 0; g < NV; ++g) {
+      if (g == qf) continue;
+      int r0, r1;
+      ridge_of<D>(r, g, qf, r0, r1);
+      unsigned h = ((unsigned)r0 * 2654435761u ^ (unsigned)(r1 + 1) * 40503u) & mask;
+      int other = -1;
+      for (int probe = 0; probe < kBigR; ++probe, h = (h + 1) & mask) {
+        if (R[4 * h] == -1) break;
+        if (R[4 * h] == r0 && R[4 * h + 1] == r1) {
+          const int a = R[4 * h + 2], b = R[4 * h + 3];
+          other = a == ((j << 2) | g) ? b : a;
+          break;
+        }
+      }
+      if (other < 0) {
+        set_error(T.ctr, E_INTERNAL);
+        continue;
+      }
+      const int m = other >> 2;
+      const int* w = FR + 6 * m;
+      // face of m opposite its vertex outside the ridge (and not the new vertex)
+      const int qm = w[5] & 3;
+      int pos = -1;
+      for (int i = 0; i < NV; ++i)
+        if (i != qm && w[i] != r0 && w[i] != r1) pos = i;
+      if (pos < 0) {
+        set_error(T.ctr, E_INTERNAL);
+        continue;
+      }
+      nn = set4(nn, g, (ID[m] << 2) | pos);
+    }
+    emit_simplex(T, r, ID[j], nn, round);
+  }
+}
+
+// Resolution pass `pass` of a round, check half.  A candidate wins iff it
+// holds every claim on its cavity, no lower candidate rewrites a face of its
+// cavity (claim_n), and no lower candidate's cavity holds one of its outer
+// neighbours.  Winners are pairwise independent (disjoint cavities, no
+// cavity meets another's outer shell), so a pass equals inserting its
+// winners one after the other.  Losers stay pending; k_reclaim lets those
+// whose region no winner of this round touched claim again, so candidates
+// that lost only to other losers still get in (winners grow toward a
+// maximal independent set).
+//
+// Slots: the new simplex built on a boundary facet of cavity simplex k reuses
+// the slot of k when it is the first facet of k, so a point that was inside
+// k usually finds itself in (or next to) the simplex now in k's slot.
+template <int D>
+__global__ void __launch_bounds__(128) k_check(DevTree T, int round, int pass, int last) {
+  constexpr int MAXF = Cap<D>::MAXF, MAXC = Cap<D>::MAXC;
+  __shared__ WarpCommit<D> smem[4];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WarpCommit<D>& W = smem[wib];
+  const int nc = min(T.ctr->ncand, T.cap_cand);
+  const unsigned long long pe = pass_epoch(round, pass);
+  const int par = round & 1;
+  unsigned long long nwon = 0, ncreated = 0, nkilled = 0;
+  int nholes = 0;
+  // fresh simplex slots come from a per-warp chunk kept across launches
+  const int gw = blockIdx.x * 4 + wib;
+  int2 chunk = gw < T.cap_wchunk ? T.wchunk[gw] : make_int2(0, 0);
+  for (int sb = (blockIdx.x * 4 + wib) * 32; sb < nc; sb += gridDim.x * 4 * 32) {
+    const bool pend = sb + lane < nc && T.cinfo[sb + lane].w == ST_OK;
+    unsigned todo = __ballot_sync(FULL, pend);
+    while (todo) {
+    const int c = sb + __ffs(todo) - 1;
+    todo &= todo - 1;
+    const int4 info = T.cinfo[c];
+    const int4 cd = T.cand[c];
+    const unsigned long long key = pe | (unsigned)cd.z;
+    int *P, *F, ncav, nfac;
+    bool big;
+    cand_lists(T, info, P, F, ncav, nfac, big);
+    bool ok = true;
+    for (int i = lane; i < ncav; i += 32) {
+      const int s = P[i];
+      if (bad_simp(T, s)) {
+        ok = false;
+        continue;
+      }
+      ok = ok && T.claim_c[s] == key && T.claim_n[s] > key;
+    }
+    for (int j = lane; j < nfac; j += 32) {
+      const int o = F[6 * j + 4];
+      if (o < 0) continue;
+      ok = ok && !bad_simp(T, o >> 2) && T.claim_c[o >> 2] > key;
+    }
+    if (!__all_sync(FULL, ok)) {
+      if (last && lane == 0) T.cinfo[c].w = ST_LOST;
+      continue;
+    }
+    const int fresh = max(0, nfac - ncav);
+    if (fresh > chunk.y) {
+      const int take = max(fresh, kSlotChunk);
+      int b0 = 0;
+      if (lane == 0) b0 = atomicAdd(&T.ctr->nsimp, take);
+      b0 = __shfl_sync(FULL, b0, 0);
+      chunk = make_int2(b0, take);
+      if (b0 + take > T.cap_simp) {
+        if (lane == 0) {
+          atomicAdd(&T.ctr->wasted, take);
+          atomicExch(&T.ctr->simp_overflow, 1);
+        }
+        chunk = make_int2(0, 0);
+      }
+    }
+    if (fresh > chunk.y) {
+      if (lane == 0) T.cinfo[c].w = ST_LOST;
+      continue;
+    }
+    const int base = chunk.x;
+    chunk.x += fresh;
+    chunk.y -= fresh;
+    for (int i = lane; i < ncav; i += 32) T.killed[P[i]] = make_int2(round, cd.x);
+    int id0;
+    if (!big && nfac <= MAXF && ncav <= MAXC) {
+      // slot assignment: first facet of cavity simplex k takes k's slot;
+      // the other facets take the remaining cavity slots, then fresh ones
+      for (int i = lane; i < ncav; i += 32) W.first[i] = 0x7fffffff;
+      for (int x = lane; x < 6 * nfac; x += 32) W.fr[x] = F[x];
+      __syncwarp();
+      for (int j = lane; j < nfac; j += 32) atomicMin(&W.first[W.fr[6 * j + 5] >> 2], j);
+      __syncwarp();
+      int nfree = 0;  // cavity slots without an own facet, ranked
+      for (int i0 = 0; i0 < ncav; i0 += 32) {
+        const int i = i0 + lane;
+        const bool fr = i < ncav && W.first[i] == 0x7fffffff;
+        const unsigned m = __ballot_sync(FULL, fr);
+        if (fr) W.freeslot[nfree + __popc(m & ((1u << lane) - 1))] = P[i];
+        nfree += __popc(m);
+      }
+      int nsec = 0;  // facets that are not the first of their cavity simplex
+      for (int j0 = 0; j0 < nfac; j0 += 32) {
+        const int j = j0 + lane;
+        int id = 0;
+        bool sec = false;
+        if (j < nfac) {
+          const int k = W.fr[6 * j + 5] >> 2;
+          sec = W.first[k] != j;
+          if (!sec) id = P[k];
+        }
+        const unsigned m = __ballot_sync(FULL, sec);
+        if (sec) {
+          const int t = nsec + __popc(m & ((1u << lane) - 1));
+          id = t < nfree ? W.freeslot[t] : base + (t - nfree);
+        }
+        if (j < nfac) W.id[j] = id;
+        nsec += __popc(m);
+      }
+      __syncwarp();
+      id0 = W.id[0];
+      // leftover cavity slots become holes pointing into the star
+      for (int t = nsec + lane; t < nfree; t += 32)
+        store_simplex(T, W.freeslot[t], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
+      write_star<D>(T, W.fr, W.id, nfac, cd.x, round, lane);
+    } else {
+      // large star (spilled search): plain slot assignment, ids in the
+      // stretch's vertex-list area (free after the search), ridge table in
+      // its own area
+      int* ID = P + kOffCV;
+      for (int j = lane; j < nfac; j += 32) ID[j] = j < ncav ? P[j] : base + (j - ncav);
+      __syncwarp();
+      id0 = ID[0];
+      for (int i = nfac + lane; i < ncav; i += 32)
+        store_simplex(T, P[i], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
+      write_star_big<D>(T, F, ID, nfac, round, P + kOffR, lane);
+    }
+    if (lane == 0) {
+      write_hints<D>(T, load_pt(T, cd.x), id0);
+      T.cinfo[c].w = ST_DONE;
+      T.act[par][cd.w].x = -1;
+    }
+    ++nwon;
+    ncreated += nfac;
+    nkilled += ncav;
+    nholes += max(0, ncav - nfac);
+    __syncwarp();
+    }
+  }
+  if (lane == 0) {
+    if (gw < T.cap_wchunk) T.wchunk[gw] = chunk;
+    if (nwon) {
+      atomicAdd(&T.ctr->won[min(pass, kPassesMax - 1)], nwon);
+      atomicAdd(&T.ctr->winners, (int)nwon);
+      atomicAdd(&T.ctr->ninserted, (int)nwon);
+      atomicAdd(&T.ctr->created, ncreated);
+      atomicAdd(&T.ctr->killed, nkilled);
+      if (nholes) atomicAdd(&T.ctr->holes, nholes);
+    }
+  }
+}
+
+// Resolution pass `pass` >= 1, claim half: a pending loser whose cavity holds
+// a simplex that a winner of this round removed or repointed, or whose outer
+// neighbour a winner removed, drops out for this round; the others claim
+// again with this pass's key (smaller than every earlier key of the round).
+template <int D>
+__global__ void __launch_bounds__(128) k_reclaim(DevTree T, int round, int pass) {
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nc = min(T.ctr->ncand, T.cap_cand);
+  const unsigned long long pe = pass_epoch(round, pass);
+  for (int sb = (blockIdx.x * 4 + wib) * 32; sb < nc; sb += gridDim.x * 4 * 32) {
+    const bool pend = sb + lane < nc && T.cinfo[sb + lane].w == ST_OK;
+    unsigned todo = __ballot_sync(FULL, pend);
+    while (todo) {
+    const int c = sb + __ffs(todo) - 1;
+    todo &= todo - 1;
+    const int4 info = T.cinfo[c];
+    const int4 cd = T.cand[c];
+    int *P, *F, ncav, nfac;
+    bool big;
+    cand_lists(T, info, P, F, ncav, nfac, big);
+    bool blocked = false;
+    for (int i = lane; i < ncav; i += 32) {
+      const int s = P[i];
+      blocked = blocked || T.killed[s].x == round || T.touched[s] == round;
+    }
+    for (int j = lane; j < nfac; j += 32) {
+      const int o = F[6 * j + 4];
+      if (o >= 0) blocked = blocked || T.killed[o >> 2].x == round;
+    }
+    if (__any_sync(FULL, blocked)) {
+      if (lane == 0) T.cinfo[c].w = ST_LOST;
+      continue;
+    }
+    claim_region(T, P, ncav, F, nfac, pe | (unsigned)cd.z, lane);
+    }
+  }
+}
+
+template <int D>
+__global__ void k_relocate(DevTree T, int round) {
+  constexpr int NV = D + 1;
+  const int par = round & 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    T.ctr->ncand = 0;
+    T.ctr->pool_used = 0;
+  }
+  const int n = T.ctr->nact[par];
+  const unsigned long long ep1 = epoch(round + 1);
+  vdp::Tally tl = {0, 0, 0, 0};
+  int perr = 0;
+  unsigned long long walk = 0;
+  const int cap = 4096;
+  for (int b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+    const int i = b + threadIdx.x;
+    bool keep = false;
+    int4 e = make_int4(-1, -1, 0, 0);
+    if (i < n) {
+      e = T.act[par][i];
+      if (e.x >= 0) {
+        keep = true;
+        if (bad_simp(T, e.y)) {
+          set_error(T.ctr, E_INTERNAL);
+          e.y = 0;
+        }
+        const int2 kr = T.killed[e.y];
+        if (kr.x == round) {
+          int cur = e.y;
+          int4 v, nn;
+          load_simplex(T, cur, v, nn);
+          if (v.x < 0) {
+            cur = nn.x >> 2;
+            if (nn.x < 0 || bad_simp(T, cur)) {
+              set_error(T.ctr, E_INTERNAL);
+              cur = e.y;
+            }
+            load_simplex(T, cur, v, nn);
+          }
+          const vdp::FPt fp = load_fpt(T, e.x);
+          int step = 0;
+          for (; step < cap; ++step) {
+            int qpos = 0;
+            for (int j = 0; j < NV; ++j)
+              if (get4(v, j) == kr.y) qpos = j;
+            vdp::FPt fv[NV];
+            for (int j = 0; j < NV; ++j) fv[j] = load_fpt(T, get4(v, j));
+            const unsigned mask = ((1u << NV) - 1) & ~(1u << qpos);
+            auto load64 = [&](vdp::VPt* v64, vdp::VPt& p64) {
+              for (int j = 0; j < NV; ++j) v64[j] = load_pt(T, get4(v, j));
+              p64 = load_pt(T, e.x);
+            };
+            const int f = vdp::exit_face_hl<D>(fv, fp, mask, tl, perr, load64);
+            if (f < 0) break;
+            cur = get4(nn, f) >> 2;
+            if (get4(nn, f) < 0 || bad_simp(T, cur)) {
+              set_error(T.ctr, E_INTERNAL);
+              cur = e.y;
+              break;
+            }
+            load_simplex(T, cur, v, nn);
+            ++walk;
+          }
+          if (step == cap) set_error(T.ctr, E_WALK);
+          e.y = cur;
+        }
+      }
+    }
+    vote_min(T.vote, keep, e.y, ep1 | (unsigned)e.z);
+    const int k = warp_append(&T.ctr->nact[par ^ 1], keep);
+    if (keep) T.act[par ^ 1][k] = e;
+  }
+  if (perr) set_error(T.ctr, E_PRECISION);
+  flush_tally(T.ctr, tl, 0, walk);
+}
+
+template <int D>
+void round_impl(const DevTree& T, const Launch& L, int round, const Tuning& tu, Prof* pf) {
+  auto mark = [&](int type) {
+    if (pf && pf->n < Prof::kMax) {
+      cudaEventRecord(pf->ev[pf->n + 1], L.stream);
+      pf->type[pf->n++] = type;
+    }
+  };
+  if (pf && pf->n == 0) cudaEventRecord(pf->ev[0], L.stream);
+  k_pick<<<L.blocks, 256, 0, L.stream>>>(T, round);
+  mark(KT_PICK);
+  k_cavity<D><<<L.warps / 4, 128, 0, L.stream>>>(T, round, tu.thin);
+  mark(KT_CAVITY);
+  for (int p = 0; p < tu.passes; ++p) {
+    if (p > 0) {
+      k_reclaim<D><<<L.warps / 4, 128, 0, L.stream>>>(T, round, p);
+      mark(KT_RECLAIM);
+    }
+    k_check<D><<<L.warps / 4, 128, 0, L.stream>>>(T, round, p, p == tu.passes - 1);
+    mark(KT_CHECK);
+  }
+  k_relocate<D><<<L.blocks, 256, 0, L.stream>>>(T, round);
+  mark(KT_RELOCATE);
+}
+
+}  // namespace
+
+void launch_upload(const DevTree& T, const Launch& L, int dim, const double* d_xyz, int64_t n,
+                   int base_vid, const int* super_order) {
+  int4 sup = make_int4(super_order[0], super_order[1], super_order[2], super_order[3]);
+  if (dim == 3)
+    k_upload<3><<<L.blocks, 256, 0, L.stream>>>(T, d_xyz, n, base_vid, sup);
+  else
+    k_upload<2><<<L.blocks, 256, 0, L.stream>>>(T, d_xyz, n, base_vid, sup);
+}
+
+void launch_prefix_hist(const Launch& L, int64_t n, int base_vid, uint64_t seed,
+                        const unsigned long long* thr, int nthr, int* d_counts) {
+  Thresholds th;
+  th.n = nthr;
+  for (int k = 0; k < kMaxPrefixes; ++k) th.t[k] = k < nthr ? thr[k] : ~0ull;
+  k_prefix_hist<<<L.blocks, 256, 0, L.stream>>>(n, base_vid, seed, th, d_counts);
+}
+
+void launch_activate(const DevTree& T, const Launch& L, int dim, int64_t n, int base_vid, uint64_t seed,
+                     unsigned long long lo, unsigned long long hi, int round) {
+  if (dim == 3)
+    k_activate<3><<<L.blocks, 256, 0, L.stream>>>(T, n, base_vid, seed, lo, hi, round);
+  else
+    k_activate<2><<<L.blocks, 256, 0, L.stream>>>(T, n, base_vid, seed, lo, hi, round);
+}
+
+void launch_round(const DevTree& T, const Launch& L, int dim, int round, const Tuning& tu, Prof* pf) {
+  if (dim == 3)
+    round_impl<3>(T, L, round, tu, pf);
+  else
+    round_impl<2>(T, L, round, tu, pf);
+}
+
+const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_cavity",   "k_check", "k_reclaim",
+                                                "k_relocate", "k_activate", "edges"};
+
+}  // namespace vd

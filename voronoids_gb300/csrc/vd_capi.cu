@@ -1,0 +1,961 @@
+// Host runtime behind the C ABI (include/voronoids_gpu.h).
+//
+// Owns the device pools of one tree, sizes them, drives the insertion rounds
+// on the tree's stream and converts results to the reference's shapes.  The
+// only host<->device synchronisations during a build are one counter read
+// every few rounds (to stop, to grow a pool, or to report an error).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../../include/voronoids_gpu.h"
+#include "vd_common.cuh"
+
+namespace vd {
+int64_t run_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_in,
+                  const EdgeScratch& S, uint2* d_out, int* d_total_pair, int* h_total_pair);
+}
+
+namespace {
+
+using vd::Counters;
+using vd::DevTree;
+
+// ---------------------------------------------------------------------------
+// Reference super simplex, restated bit for bit (host code is compiled with
+// -ffp-contract=off so each operation rounds as in Rust).
+//   bounding_sphere: src/geometry.rs:99-142
+//   3D vertices:     src/delaunay_tree.rs:392-406
+//   2D vertices:     src/delaunay_tree.rs:547-558
+// ---------------------------------------------------------------------------
+bool ref_in_sphere(const double* v, const double* c, double r, int dim) {
+  double d = 0.0;
+  for (int i = 0; i < dim; ++i) d += (c[i] - v[i]) * (c[i] - v[i]);
+  return d < r * r;
+}
+
+void ref_bounding_sphere(int dim, const double* pts, int64_t n, double* center, double* radius) {
+  double lo[3], hi[3];
+  for (int i = 0; i < dim; ++i) {
+    double l = INFINITY, h = -INFINITY;
+    for (int64_t k = 0; k < n; ++k) {
+      const double v = pts[k * dim + i];
+      l = fmin(l, v);
+      h = fmax(h, v);
+    }
+    lo[i] = l;
+    hi[i] = h;
+    center[i] = (h + l) / 2.0;
+  }
+  double su = 0.0, sl = 0.0;
+  for (int i = 0; i < dim; ++i) su += (hi[i] - center[i]) * (hi[i] - center[i]);
+  for (int i = 0; i < dim; ++i) sl += (lo[i] - center[i]) * (lo[i] - center[i]);
+  const double ud = sqrt(su), ld = sqrt(sl);
+  double r = ud > ld ? ud : ld;
+  for (int64_t k = 0; k < n; ++k)
+    if (!ref_in_sphere(pts + k * dim, center, r, dim)) r = r * 1.5;
+  *radius = r;
+}
+
+void ref_super_vertices(int dim, const double* pts, int64_t n, double out[4][3], double* R) {
+  double c[3] = {0, 0, 0}, r;
+  ref_bounding_sphere(dim, pts, n, c, &r);
+  r *= 10.0;
+  *R = r;
+  const double pi = 3.141592653589793;
+  const double c1 = cos(2. * pi / 3.), s1 = sin(2. * pi / 3.);
+  const double c2 = cos(4. * pi / 3.), s2 = sin(4. * pi / 3.);
+  if (dim == 3) {
+    const double v[4][3] = {{c[0], c[1], c[2] + r},
+                            {c[0] + r, c[1], c[2] - r},
+                            {c[0] + r * c1, c[1] + r * s1, c[2] - r},
+                            {c[0] + r * c2, c[1] + r * s2, c[2] - r}};
+    memcpy(out, v, sizeof(v));
+  } else {
+    const double v[3][3] = {
+        {c[0] + r, c[1], 0.0}, {c[0] + r * c1, c[1] + r * s1, 0.0}, {c[0] + r * c2, c[1] + r * s2, 0.0}};
+    memcpy(out, v, sizeof(v));
+    out[3][0] = out[3][1] = out[3][2] = 0.0;
+  }
+}
+
+bool coord_ok(double a) {
+  a = fabs(a);
+  return a == 0.0 || (a >= 7.006492321624085e-46 && a <= 1.4272476927059599e45);
+}
+
+template <class T>
+int dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void**)p, sizeof(T) * count) == cudaSuccess ? vd::E_OK : vd::E_NOMEM;
+}
+
+template <class T>
+void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+}  // namespace
+
+struct vd_tree {
+  int dim = 3;
+  int ns = 4;
+  int device = 0;
+  int sms = 1;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  double sup[4][3] = {};
+  double R = 0;
+  int sup_order[4] = {0, 1, 2, 3};
+  int64_t nverts = 0;     // super + inserted/pending vertices
+  int64_t cap_verts = 0;
+  int64_t cap_act = 0;
+  int round = 0;
+  int64_t inserted = 0;   // vertices inserted (from counters)
+  int64_t calls = 0;
+  DevTree T = {};
+  Counters* hctr = nullptr;   // pinned host mirror
+  // edges
+  bool edges_valid = false;
+  int64_t nedges = 0;
+  uint2* d_edges = nullptr;
+  int64_t cap_edges = 0;
+  vd::EdgeScratch es = {};
+  int64_t es_n = -1;
+  int* d_pair = nullptr;
+  int* h_pair = nullptr;
+  unsigned long long* d_check = nullptr;
+  int* d_misc = nullptr;      // small device scratch (live-slot search, locate)
+  int64_t* d_loc = nullptr;
+  int64_t cap_loc = 0;
+  // insertion schedule (priority prefixes)
+  int64_t first_prefix = 64;
+  double growth = 4.0;
+  int* d_counts = nullptr;
+  int* h_counts = nullptr;
+  // profiling: per-kernel time from CUDA events on the tree's stream
+  bool prof = false;
+  std::vector<vd::Prof> profs;   // one event log per round of a chunk
+  double kms[vd::KT_COUNT] = {};
+  int64_t kcnt[vd::KT_COUNT] = {};
+  vd::Tuning tuning = {3, 1};
+  // per-round trace (diagnostics; syncs after every round)
+  bool trace = false;
+  std::vector<int64_t> trace_rows;
+};
+
+namespace {
+
+vd::Launch launch_of(const vd_tree* t) {
+  vd::Launch L;
+  L.blocks = t->sms * 8;
+  L.warps = t->sms * 5 * 4;
+  L.stream = t->stream;
+  return L;
+}
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? vd::E_OK : vd::E_CUDA; }
+
+constexpr int kChunkMax = 16;
+
+vd::Prof* round_prof(vd_tree* t, int k) {
+  if (!t->prof) return nullptr;
+  if (t->profs.empty()) {
+    t->profs.resize(kChunkMax + 1);
+    for (auto& p : t->profs)
+      for (auto& e : p.ev) cudaEventCreate(&e);
+  }
+  t->profs[k].n = 0;
+  return &t->profs[k];
+}
+
+void accumulate_events(vd_tree* t, int rounds) {
+  if (!t->prof) return;
+  for (int r = 0; r < rounds; ++r) {
+    const vd::Prof& p = t->profs[r];
+    for (int i = 0; i < p.n; ++i) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, p.ev[i], p.ev[i + 1]) == cudaSuccess) {
+        t->kms[p.type[i]] += ms;
+        t->kcnt[p.type[i]] += 1;
+      }
+    }
+  }
+}
+
+// Times one non-round kernel sequence (activation, edges) into type `kt`.
+struct ScopedProf {
+  vd_tree* t;
+  int kt;
+  vd::Prof* p;
+  ScopedProf(vd_tree* t_, int kt_) : t(t_), kt(kt_), p(round_prof(t_, kChunkMax)) {
+    if (p) cudaEventRecord(p->ev[0], t->stream);
+  }
+  ~ScopedProf() {
+    if (!p) return;
+    cudaEventRecord(p->ev[1], t->stream);
+    cudaEventSynchronize(p->ev[1]);
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p->ev[0], p->ev[1]) == cudaSuccess) {
+      t->kms[kt] += ms;
+      t->kcnt[kt] += 1;
+    }
+  }
+};
+
+int sync_counters(vd_tree* t) {
+  cudaMemcpyAsync(t->hctr, t->T.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, t->stream);
+  return cuda_status(cudaStreamSynchronize(t->stream));
+}
+
+// Grow a device array to `want` elements, keeping the first `keep` elements,
+// filling the new tail with `fill` bytes (-1 = leave uninitialised).
+template <class T>
+int grow(T** p, int64_t* cap, int64_t want, int64_t keep, int fill, cudaStream_t st) {
+  if (want <= *cap) return vd::E_OK;
+  T* np = nullptr;
+  if (dalloc(&np, (size_t)want) != vd::E_OK) return vd::E_NOMEM;
+  if (*p && keep > 0) cudaMemcpyAsync(np, *p, sizeof(T) * keep, cudaMemcpyDeviceToDevice, st);
+  if (fill >= 0) cudaMemsetAsync(np + keep, fill, sizeof(T) * (want - keep), st);
+  if (*p) {
+    cudaStreamSynchronize(st);
+    cudaFree(*p);
+  }
+  *p = np;
+  *cap = want;
+  return vd::E_OK;
+}
+
+int ensure_simplices(vd_tree* t, int64_t want) {
+  int64_t cap = t->T.cap_simp;
+  if (want <= cap) return vd::E_OK;
+  want = std::max(want, cap + cap / 2);
+  if (want > (int64_t(1) << 29)) return vd::E_NOMEM;  // neighbour codes use 30 bits
+  int64_t used = t->hctr->nsimp;
+  int64_t c[7] = {cap, cap, cap, cap, cap, cap, cap};
+  int rc = vd::E_OK;
+  rc |= grow(&t->T.simp, &c[0], want, used, 0xff, t->stream);
+  rc |= grow(&t->T.vote, &c[1], want, used, 0xff, t->stream);
+  rc |= grow(&t->T.thin, &c[2], want, used, 0xff, t->stream);
+  rc |= grow(&t->T.claim_c, &c[3], want, used, 0xff, t->stream);
+  rc |= grow(&t->T.claim_n, &c[4], want, used, 0xff, t->stream);
+  rc |= grow(&t->T.killed, &c[5], want, used, 0xff, t->stream);
+  rc |= grow(&t->T.touched, &c[6], want, used, 0xff, t->stream);
+  if (rc) return vd::E_NOMEM;
+  t->T.cap_simp = (int)want;
+  return vd::E_OK;
+}
+
+int ensure_points(vd_tree* t, int64_t n_new) {
+  int64_t want = t->nverts + n_new;
+  if (want > 0x7ffffff0LL) return vd::E_ARG;
+  int64_t cap = t->cap_verts;
+  if (want > cap) {
+    int64_t target = std::max(want, cap + cap / 2);
+    int64_t cap2 = t->cap_verts;
+    if (grow(&t->T.pts, &cap, target, t->nverts, -1, t->stream)) return vd::E_NOMEM;
+    if (grow(&t->T.ptf, &cap2, target, t->nverts, -1, t->stream)) return vd::E_NOMEM;
+    t->cap_verts = cap;
+    t->T.cap_verts = (int)cap;
+  }
+  if (n_new > t->cap_act) {
+    int64_t c = std::max<int64_t>(n_new, 1024);
+    dfree(t->T.act[0]);
+    dfree(t->T.act[1]);
+    dfree(t->T.cand);
+    dfree(t->T.cinfo);
+    if (dalloc(&t->T.act[0], c) || dalloc(&t->T.act[1], c) || dalloc(&t->T.cand, c) ||
+        dalloc(&t->T.cinfo, c))
+      return vd::E_NOMEM;
+    t->cap_act = c;
+    t->T.cap_cand = (int)c;
+  }
+  const int64_t pool_want = std::min<int64_t>(
+      std::max<int64_t>((t->dim == 3 ? 48 : 24) * std::max<int64_t>(n_new, 1024), 8 * 360448 + 64),
+      0x7fffffffLL);
+  if (pool_want > t->T.cap_pool) {
+    dfree(t->T.pool);
+    if (dalloc(&t->T.pool, pool_want)) return vd::E_NOMEM;
+    t->T.cap_pool = (int)pool_want;
+  }
+  const int64_t dup_want = t->hctr->ndup + n_new;
+  if (dup_want > t->T.cap_dups) {
+    int64_t cap_d = t->T.cap_dups;
+    if (grow(&t->T.dups, &cap_d, std::max(dup_want, cap_d * 2), std::min<int64_t>(t->hctr->ndup, cap_d),
+             -1, t->stream))
+      return vd::E_NOMEM;
+    t->T.cap_dups = (int)cap_d;
+  }
+  return vd::E_OK;
+}
+
+void release(vd_tree* t) {
+  if (!t) return;
+  if (t->stream) cudaStreamSynchronize(t->stream);
+  dfree(t->T.pts);
+  dfree(t->T.ptf);
+  dfree(t->T.simp);
+  dfree(t->T.vote);
+  dfree(t->T.thin);
+  dfree(t->T.claim_c);
+  dfree(t->T.claim_n);
+  dfree(t->T.touched);
+  dfree(t->T.killed);
+  dfree(t->T.act[0]);
+  dfree(t->T.act[1]);
+  dfree(t->T.cand);
+  dfree(t->T.cinfo);
+  dfree(t->T.pool);
+  dfree(t->T.dups);
+  dfree(t->T.ctr);
+  dfree(t->d_edges);
+  dfree(t->es.cnt);
+  dfree(t->es.off);
+  dfree(t->es.buf);
+  dfree(t->es.ucnt);
+  dfree(t->es.uoff);
+  dfree(t->es.big);
+  dfree(t->es.nbig);
+  dfree(t->es.scan_tmp);
+  dfree(t->d_pair);
+  dfree(t->d_check);
+  dfree(t->d_misc);
+  dfree(t->d_loc);
+  dfree(t->d_counts);
+  dfree(t->T.hint);
+  dfree(t->T.wchunk);
+  if (t->h_counts) cudaFreeHost(t->h_counts);
+  t->h_counts = nullptr;
+  if (t->hctr) cudaFreeHost(t->hctr);
+  if (t->h_pair) cudaFreeHost(t->h_pair);
+  t->hctr = nullptr;
+  t->h_pair = nullptr;
+  for (auto& p : t->profs)
+    for (auto& e : p.ev) cudaEventDestroy(e);
+  t->profs.clear();
+  if (t->own_stream && t->stream) cudaStreamDestroy(t->stream);
+  t->stream = nullptr;
+}
+
+int init_tree(vd_tree* t, int dim, const double* pts, int64_t n, void* stream) {
+  if ((dim != 2 && dim != 3) || n < 1 || !pts) return vd::E_ARG;
+  for (int64_t i = 0; i < n * dim; ++i) {
+    if (!isfinite(pts[i])) return vd::E_NONFINITE;
+    if (!coord_ok(pts[i])) return vd::E_RANGE;
+  }
+  t->dim = dim;
+  t->ns = dim + 1;
+  ref_super_vertices(dim, pts, n, t->sup, &t->R);
+  if (!(t->R > 0.0) || !isfinite(t->R)) return vd::E_DEGENERATE;
+  for (int i = 0; i < t->ns; ++i)
+    for (int j = 0; j < 3; ++j)
+      if (!isfinite(t->sup[i][j]) || !coord_ok(t->sup[i][j])) return vd::E_RANGE;
+  // positive orientation of the super simplex
+  {
+    vdp::VPt v[4];
+    for (int i = 0; i < 4; ++i) v[i] = vdp::VPt{t->sup[i][0], t->sup[i][1], t->sup[i][2], 0.0};
+    vdp::Tally tl = {0, 0, 0, 0};
+    int err = 0;
+    int neg = dim == 3 ? vdp::exit_face<3, true>(v, v[3], 1u << 3, tl, err)
+                       : vdp::exit_face<2, true>(v, v[2], 1u << 2, tl, err);
+    if (neg >= 0) {
+      // orientation <= 0: swap the first two (zero would be degenerate)
+      std::swap(t->sup_order[0], t->sup_order[1]);
+      vdp::VPt w[4] = {v[1], v[0], v[2], v[3]};
+      int neg2 = dim == 3 ? vdp::exit_face<3, true>(w, w[3], 1u << 3, tl, err)
+                          : vdp::exit_face<2, true>(w, w[2], 1u << 2, tl, err);
+      if (neg2 >= 0) return vd::E_DEGENERATE;
+    }
+    if (dim == 2) t->sup_order[3] = -1;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return vd::E_CUDA;
+  t->device = dev;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  t->sms = std::max(sms, 1);
+  if (stream) {
+    t->stream = (cudaStream_t)stream;
+    t->own_stream = false;
+  } else {
+    if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) return vd::E_CUDA;
+    t->own_stream = true;
+  }
+  if (cudaMallocHost((void**)&t->hctr, sizeof(Counters)) != cudaSuccess) return vd::E_NOMEM;
+  if (cudaMallocHost((void**)&t->h_pair, 4 * sizeof(int)) != cudaSuccess) return vd::E_NOMEM;
+  memset(t->hctr, 0, sizeof(Counters));
+  if (dalloc(&t->T.ctr, 1) || dalloc(&t->d_pair, 4) || dalloc(&t->d_check, 8) ||
+      dalloc(&t->d_misc, 16) || dalloc(&t->d_counts, vd::kMaxPrefixes))
+    return vd::E_NOMEM;
+  if (cudaMallocHost((void**)&t->h_counts, sizeof(int) * vd::kMaxPrefixes) != cudaSuccess) return vd::E_NOMEM;
+  t->T.cap_wchunk = t->sms * 20;
+  if (dalloc(&t->T.wchunk, t->T.cap_wchunk)) return vd::E_NOMEM;
+  cudaMemsetAsync(t->T.wchunk, 0, sizeof(int2) * t->T.cap_wchunk, t->stream);
+  // hint grid over the sizing box (centre +- bounding radius)
+  t->T.hint_levels = dim == 3 ? 6 : 9;
+  const int64_t ncells = dim == 3 ? ((1LL << (3 * (t->T.hint_levels + 1))) - 1) / 7
+                                  : ((1LL << (2 * (t->T.hint_levels + 1))) - 1) / 3;
+  if (dalloc(&t->T.hint, ncells)) return vd::E_NOMEM;
+  cudaMemsetAsync(t->T.hint, 0xff, sizeof(int) * ncells, t->stream);
+  {
+    double c[3] = {0, 0, 0}, rb = 0;
+    ref_bounding_sphere(dim, pts, n, c, &rb);
+    for (int k = 0; k < 3; ++k) t->T.gorg[k] = (k < dim ? c[k] : 0.0) - rb;
+    t->T.gscale = rb > 0 ? 1.0 / (2.0 * rb) : 1.0;
+  }
+  cudaMemsetAsync(t->T.ctr, 0, sizeof(Counters), t->stream);
+  // vertices: super first
+  t->cap_verts = t->ns + std::max<int64_t>(n, 16);
+  if (dalloc(&t->T.pts, t->cap_verts) || dalloc(&t->T.ptf, t->cap_verts)) return vd::E_NOMEM;
+  t->T.cap_verts = (int)t->cap_verts;
+  std::vector<vdp::VPt> sv(t->ns);
+  for (int i = 0; i < t->ns; ++i) sv[i] = vdp::VPt{t->sup[i][0], t->sup[i][1], t->sup[i][2], 0.0};
+  cudaMemcpyAsync(t->T.pts, sv.data(), sizeof(vdp::VPt) * t->ns, cudaMemcpyHostToDevice, t->stream);
+  std::vector<vdp::FPt> sf(t->ns);
+  for (int i = 0; i < t->ns; ++i) sf[i] = vdp::split_point(t->sup[i][0], t->sup[i][1], t->sup[i][2]);
+  cudaMemcpyAsync(t->T.ptf, sf.data(), sizeof(vdp::FPt) * t->ns, cudaMemcpyHostToDevice, t->stream);
+  t->nverts = t->ns;
+  // simplex pool with the super simplex in slot 0
+  t->T.cap_simp = 0;
+  t->hctr->nsimp = 0;
+  t->hctr->nsimp = 0;
+  if (ensure_simplices(t, 1024)) return vd::E_NOMEM;
+  vd::Simplex s0;
+  for (int i = 0; i < 4; ++i) {
+    s0.v[i] = t->sup_order[i];
+    s0.n[i] = -1;
+  }
+  cudaMemcpyAsync(t->T.simp, &s0, sizeof(s0), cudaMemcpyHostToDevice, t->stream);
+  Counters init;
+  memset(&init, 0, sizeof(init));
+  init.nsimp = 1;
+  *t->hctr = init;
+  cudaMemcpyAsync(t->T.ctr, &init, sizeof(init), cudaMemcpyHostToDevice, t->stream);
+  return cuda_status(cudaStreamSynchronize(t->stream));
+}
+
+vd::Launch sized_launch(const vd_tree* t, int64_t items) {
+  vd::Launch L = launch_of(t);
+  const int64_t blocks = (items + 255) / 256;
+  L.blocks = (int)std::max<int64_t>(1, std::min<int64_t>(blocks, L.blocks));
+  const int64_t warps = ((items + 3) / 4) * 4;
+  L.warps = (int)std::max<int64_t>(4, std::min<int64_t>(warps, L.warps));
+  return L;
+}
+
+// Runs insertion rounds until at most `stop` points are still active.
+int run_rounds(vd_tree* t, const vd::Launch& L, int& r, int64_t stop) {
+  int chunk = 2;
+  int64_t last_progress = -1;
+  int stalled = 0;
+  int rc = vd::E_OK;
+  while (true) {
+    if (t->trace) chunk = 1;
+    for (int k = 0; k < chunk; ++k) vd::launch_round(t->T, L, t->dim, r++, t->tuning, round_prof(t, k));
+    rc = sync_counters(t);
+    if (rc) break;
+    accumulate_events(t, chunk);
+    Counters& h = *t->hctr;
+    if (t->trace) {
+      const int64_t row[8] = {r - 1,
+                              (int64_t)h.nact[(r - 1) & 1],
+                              (int64_t)h.candidates,
+                              (int64_t)h.searched,
+                              (int64_t)h.ninserted,
+                              (int64_t)h.cavity_tests,
+                              (int64_t)h.walk,
+                              (int64_t)h.nact[r & 1]};
+      t->trace_rows.insert(t->trace_rows.end(), row, row + 8);
+    }
+    if (h.err) {
+      rc = h.err;
+      break;
+    }
+    if (h.nact[r & 1] <= stop) break;
+    // grow pools when a round had to defer work
+    bool fix = false;
+    if (h.simp_overflow || (double)h.nsimp > 0.85 * t->T.cap_simp) {
+      h.nsimp -= h.wasted;
+      h.wasted = 0;
+      h.simp_overflow = 0;
+      int64_t want = (int64_t)t->T.cap_simp + std::max<int64_t>(t->T.cap_simp / 2, 4096);
+      rc = ensure_simplices(t, want);
+      if (rc) break;
+      fix = true;
+    }
+    if (h.pool_overflow) {
+      int64_t want = std::min<int64_t>((int64_t)t->T.cap_pool * 2, 0x7fffffffLL);
+      dfree(t->T.pool);
+      if (dalloc(&t->T.pool, want)) {
+        rc = vd::E_NOMEM;
+        break;
+      }
+      t->T.cap_pool = (int)want;
+      h.pool_overflow = 0;
+      fix = true;
+    }
+    if (fix) cudaMemcpyAsync(t->T.ctr, &h, sizeof(Counters), cudaMemcpyHostToDevice, t->stream);
+    const int64_t progress = (int64_t)h.ninserted + h.ndup;
+    if (progress == last_progress) {
+      if (++stalled >= 8) {
+        rc = h.overflow ? vd::E_CAVITY : vd::E_ROUND_LIMIT;
+        break;
+      }
+    } else {
+      stalled = 0;
+      last_progress = progress;
+    }
+    chunk = std::min(chunk * 2, kChunkMax);
+  }
+  return rc;
+}
+
+// Insertion of n points already in device memory.  Points are inserted in
+// priority prefixes (first `first_prefix` points, then geometrically growing
+// by `growth`): only the points of the current prefix are located, relocated
+// and nominated, so early rounds, which can only insert a few points into a
+// small triangulation, do not pay for the whole input.  Each prefix is
+// located by walks from the hint grid and then inserted in rounds.
+int insert_device(vd_tree* t, const double* d_xyz, int64_t n, uint64_t seed) {
+  if (n < 0 || (n > 0 && !d_xyz)) return vd::E_ARG;
+  if (n == 0) return vd::E_OK;
+  int rc = ensure_points(t, n);
+  if (rc) return rc;
+  const double per = t->dim == 3 ? 7.6 : 2.3;
+  rc = ensure_simplices(t, t->hctr->nsimp + (int64_t)(per * (double)n) + 4096 + 32LL * t->T.cap_wchunk);
+  if (rc) return rc;
+  t->edges_valid = false;
+  const vd::Launch L = launch_of(t);
+  const int base = (int)t->nverts;
+  vd::launch_upload(t->T, L, t->dim, d_xyz, n, base, t->sup_order);
+  // priority thresholds of the prefixes
+  std::vector<unsigned long long> thr;
+  {
+    double m = std::min<double>((double)std::max<int64_t>(t->first_prefix, 1), (double)n);
+    const unsigned long long top = 1ull << 32;
+    while ((int)thr.size() < vd::kMaxPrefixes - 1) {
+      const double f = m / (double)n;
+      if (f >= 1.0) break;
+      thr.push_back((unsigned long long)(f * 4294967296.0));
+      m *= std::max(1.5, t->growth);
+    }
+    thr.push_back(top);
+  }
+  cudaMemsetAsync(t->d_counts, 0, sizeof(int) * vd::kMaxPrefixes, t->stream);
+  vd::launch_prefix_hist(L, n, base, seed, thr.data(), (int)thr.size(), t->d_counts);
+  cudaMemcpyAsync(t->h_counts, t->d_counts, sizeof(int) * vd::kMaxPrefixes, cudaMemcpyDeviceToHost, t->stream);
+  rc = sync_counters(t);
+  if (rc) return rc;
+  if (t->hctr->err) return t->hctr->err;
+  t->nverts += n;
+  t->calls++;
+  int r = t->round;
+  // The next prefix is activated once the current one is down to its tail
+  // (a tenth of it), so the tail's rounds also insert the next prefix.
+  int last = -1;
+  for (size_t k = 0; k < thr.size(); ++k)
+    if (t->h_counts[k] > 0) last = (int)k;
+  int64_t carried = 0;
+  for (size_t k = 0; k < thr.size() && !rc; ++k) {
+    const int cnt = t->h_counts[k];
+    if (cnt == 0) continue;
+    const unsigned long long lo = k ? thr[k - 1] : 0ull;
+    {
+      ScopedProf sp(t, vd::KT_ACTIVATE);
+      vd::launch_activate(t->T, L, t->dim, n, base, seed, lo, thr[k], r);
+    }
+    const int64_t stop = (int)k == last ? 0 : cnt / 10;
+    rc = run_rounds(t, sized_launch(t, cnt + carried), r, stop);
+    carried = t->hctr->nact[r & 1];
+  }
+  t->round = r;
+  if (!rc) rc = sync_counters(t);
+  t->inserted = t->hctr->ninserted;
+  if (rc) return rc;
+  if (t->hctr->err) return t->hctr->err;
+  return vd::E_OK;
+}
+
+int insert_host(vd_tree* t, const double* pts, int64_t n, uint64_t seed) {
+  if (n < 0 || (n > 0 && !pts)) return vd::E_ARG;
+  if (n == 0) return vd::E_OK;
+  double* d = nullptr;
+  if (dalloc(&d, (size_t)n * t->dim)) return vd::E_NOMEM;
+  cudaMemcpyAsync(d, pts, sizeof(double) * n * t->dim, cudaMemcpyHostToDevice, t->stream);
+  int rc = insert_device(t, d, n, seed);
+  cudaStreamSynchronize(t->stream);
+  cudaFree(d);
+  return rc;
+}
+
+int ensure_edge_scratch(vd_tree* t, int64_t n_in, int64_t nsimp) {
+  const int64_t buf_want = (t->dim == 3 ? 6 : 3) * nsimp + 64;
+  if (t->es_n < n_in) {
+    dfree(t->es.cnt);
+    dfree(t->es.off);
+    dfree(t->es.ucnt);
+    dfree(t->es.uoff);
+    dfree(t->es.big);
+    dfree(t->es.nbig);
+    dfree(t->es.scan_tmp);
+    const int64_t m = n_in + 2;
+    if (dalloc(&t->es.cnt, m) || dalloc(&t->es.off, m) || dalloc(&t->es.ucnt, m) ||
+        dalloc(&t->es.uoff, m) || dalloc(&t->es.big, m) || dalloc(&t->es.nbig, 1) ||
+        dalloc(&t->es.scan_tmp, vd::scan_scratch_ints(m)))
+      return vd::E_NOMEM;
+    t->es_n = n_in;
+  }
+  if (t->es.cap_buf < buf_want) {
+    dfree(t->es.buf);
+    if (dalloc(&t->es.buf, buf_want)) return vd::E_NOMEM;
+    t->es.cap_buf = buf_want;
+  }
+  if (t->cap_edges < buf_want) {
+    dfree(t->d_edges);
+    if (dalloc(&t->d_edges, buf_want)) return vd::E_NOMEM;
+    t->cap_edges = buf_want;
+  }
+  return vd::E_OK;
+}
+
+int compute_edges(vd_tree* t) {
+  if (t->edges_valid) return vd::E_OK;
+  int rc = sync_counters(t);
+  if (rc) return rc;
+  const int64_t n_in = t->nverts - t->ns;
+  const int64_t nsimp = t->hctr->nsimp;
+  if ((t->dim == 3 ? 6 : 3) * nsimp > 0x7fffff00LL) return vd::E_NOMEM;
+  rc = ensure_edge_scratch(t, n_in, nsimp);
+  if (rc) return rc;
+  int64_t m;
+  {
+    ScopedProf sp(t, vd::KT_EDGES);
+    m = vd::run_edges(t->T, launch_of(t), t->dim, (int)nsimp, (int)n_in, t->es, t->d_edges, t->d_pair,
+                      t->h_pair);
+  }
+  if (m < 0) return vd::E_CUDA;
+  t->nedges = m;
+  t->edges_valid = true;
+  return vd::E_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* vd_status_str(int s) {
+  switch (s) {
+    case VD_OK: return "ok";
+    case VD_ERR_ARG: return "invalid argument";
+    case VD_ERR_CUDA: return "CUDA runtime error";
+    case VD_ERR_NOMEM: return "device allocation failed";
+    case VD_ERR_DUPLICATE: return "duplicate points were skipped";
+    case VD_ERR_NONFINITE: return "non-finite coordinate";
+    case VD_ERR_OUTSIDE: return "point not strictly inside the super simplex";
+    case VD_ERR_PRECISION: return "exact arithmetic capacity exceeded";
+    case VD_ERR_ROUND_LIMIT: return "insertion rounds made no progress";
+    case VD_ERR_CAVITY: return "conflict region too large";
+    case VD_ERR_WALK: return "point location did not terminate";
+    case VD_ERR_INTERNAL: return "internal inconsistency";
+    case VD_ERR_DEGENERATE: return "degenerate super simplex";
+    case VD_ERR_RANGE: return "coordinate magnitude out of range";
+    default: return "unknown status";
+  }
+}
+
+vd_tree* vd_tree_new_on_stream(int dim, const double* pts, int64_t n, void* stream, int* status) {
+  vd_tree* t = new (std::nothrow) vd_tree();
+  if (!t) {
+    if (status) *status = VD_ERR_NOMEM;
+    return nullptr;
+  }
+  int rc = init_tree(t, dim, pts, n, stream);
+  if (status) *status = rc;
+  return t;
+}
+
+vd_tree* vd_tree_new(int dim, const double* pts, int64_t n, int* status) {
+  return vd_tree_new_on_stream(dim, pts, n, nullptr, status);
+}
+
+int vd_super_simplex(int dim, const double* pts, int64_t n, double* out, double* radius) {
+  if ((dim != 2 && dim != 3) || n < 1 || !pts || !out || !radius) return VD_ERR_ARG;
+  for (int64_t i = 0; i < n * dim; ++i)
+    if (!isfinite(pts[i])) return VD_ERR_NONFINITE;
+  double sv[4][3];
+  ref_super_vertices(dim, pts, n, sv, radius);
+  for (int k = 0; k <= dim; ++k)
+    for (int j = 0; j < 3; ++j) out[3 * k + j] = sv[k][j];
+  return VD_OK;
+}
+
+void vd_tree_free(vd_tree* t) {
+  if (!t) return;
+  release(t);
+  delete t;
+}
+
+static int ready(vd_tree* t) { return (t && t->hctr && t->T.ctr) ? VD_OK : VD_ERR_ARG; }
+
+int vd_insert_points_device(vd_tree* t, const double* d_pts, int64_t n, uint64_t seed) {
+  if (ready(t)) return VD_ERR_ARG;
+  int rc = insert_device(t, d_pts, n, seed);
+  if (rc == VD_OK && t->hctr->ndup > 0) rc = VD_ERR_DUPLICATE;
+  return rc;
+}
+
+int vd_insert_points(vd_tree* t, const double* pts, int64_t n, uint64_t seed) {
+  if (ready(t)) return VD_ERR_ARG;
+  int rc = insert_host(t, pts, n, seed);
+  if (rc == VD_OK && t->hctr->ndup > 0) rc = VD_ERR_DUPLICATE;
+  return rc;
+}
+
+int vd_insert_point(vd_tree* t, const double* p) { return vd_insert_points(t, p, 1, 0); }
+
+int vd_num_vertices(vd_tree* t, int64_t* n) {
+  if (ready(t) || !n) return VD_ERR_ARG;
+  *n = t->nverts - t->ns;
+  return VD_OK;
+}
+
+int vd_max_simplex_id(vd_tree* t, int64_t* id) {
+  if (ready(t) || !id) return VD_ERR_ARG;
+  int rc = sync_counters(t);
+  if (rc) return rc;
+  *id = (int64_t)t->ns + (int64_t)t->hctr->created;
+  return VD_OK;
+}
+
+int vd_num_simplices(vd_tree* t, int64_t* n) {
+  if (ready(t) || !n) return VD_ERR_ARG;
+  int rc = sync_counters(t);
+  if (rc) return rc;
+  *n = 1 + (int64_t)t->hctr->created - (int64_t)t->hctr->killed;
+  return VD_OK;
+}
+
+int vd_simplices(vd_tree* t, int32_t* verts, int32_t* nbrs, int64_t cap, int64_t* n) {
+  if (ready(t) || !n) return VD_ERR_ARG;
+  int rc = sync_counters(t);
+  if (rc) return rc;
+  const int64_t ns = t->hctr->nsimp;
+  std::vector<vd::Simplex> h(ns);
+  cudaMemcpyAsync(h.data(), t->T.simp, sizeof(vd::Simplex) * ns, cudaMemcpyDeviceToHost, t->stream);
+  if (cudaStreamSynchronize(t->stream) != cudaSuccess) return VD_ERR_CUDA;
+  std::vector<int32_t> remap(ns, -1);
+  int64_t k = 0;
+  for (int64_t i = 0; i < ns; ++i)
+    if (h[i].v[0] >= 0) remap[i] = (int32_t)k++;
+  *n = k;
+  if (!verts && !nbrs) return VD_OK;
+  if (cap < k) return VD_ERR_ARG;
+  const int nv = t->dim + 1;
+  int64_t r = 0;
+  for (int64_t i = 0; i < ns; ++i) {
+    if (h[i].v[0] < 0) continue;
+    for (int j = 0; j < 4; ++j) {
+      int v = j < nv ? h[i].v[j] : -1;
+      if (verts) verts[4 * r + j] = j < nv ? (v < t->ns ? -(1 + v) : v - t->ns) : -1;
+      int c = j < nv ? h[i].n[j] : -1;
+      if (nbrs) nbrs[4 * r + j] = c < 0 ? -1 : remap[c >> 2];
+    }
+    ++r;
+  }
+  return VD_OK;
+}
+
+int vd_num_edges(vd_tree* t, int64_t* n) {
+  if (ready(t) || !n) return VD_ERR_ARG;
+  int rc = compute_edges(t);
+  if (rc) return rc;
+  *n = t->nedges;
+  return VD_OK;
+}
+
+int vd_edges(vd_tree* t, int64_t* uv, int64_t cap, int64_t* n) {
+  if (ready(t)) return VD_ERR_ARG;
+  int rc = compute_edges(t);
+  if (rc) return rc;
+  if (n) *n = t->nedges;
+  if (!uv) return VD_OK;
+  if (cap < t->nedges) return VD_ERR_ARG;
+  std::vector<uint2> h(t->nedges);
+  cudaMemcpyAsync(h.data(), t->d_edges, sizeof(uint2) * t->nedges, cudaMemcpyDeviceToHost, t->stream);
+  if (cudaStreamSynchronize(t->stream) != cudaSuccess) return VD_ERR_CUDA;
+  for (int64_t i = 0; i < t->nedges; ++i) {
+    uv[2 * i] = h[i].x;
+    uv[2 * i + 1] = h[i].y;
+  }
+  return VD_OK;
+}
+
+int vd_edges_device(vd_tree* t, uint32_t* d_uv, int64_t cap, int64_t* n) {
+  if (ready(t)) return VD_ERR_ARG;
+  int rc = compute_edges(t);
+  if (rc) return rc;
+  if (n) *n = t->nedges;
+  if (!d_uv) return VD_OK;
+  if (cap < t->nedges) return VD_ERR_ARG;
+  cudaMemcpyAsync(d_uv, t->d_edges, sizeof(uint2) * t->nedges, cudaMemcpyDeviceToDevice, t->stream);
+  return cuda_status(cudaStreamSynchronize(t->stream));
+}
+
+int vd_check_delaunay(vd_tree* t, int* ok, int64_t* violations) {
+  if (ready(t) || !ok) return VD_ERR_ARG;
+  int rc = sync_counters(t);
+  if (rc) return rc;
+  vd::launch_check(t->T, launch_of(t), t->dim, t->hctr->nsimp, t->d_check);
+  unsigned long long h[6];
+  cudaMemcpyAsync(h, t->d_check, sizeof(h), cudaMemcpyDeviceToHost, t->stream);
+  rc = sync_counters(t);
+  if (rc) return rc;
+  if (violations)
+    for (int k = 0; k < 6; ++k) violations[k] = (int64_t)h[k];
+  *ok = (h[0] == 0 && h[1] == 0 && h[2] == 0 && h[3] == 0 && h[4] == (unsigned long long)(t->dim + 1)) ? 1 : 0;
+  return t->hctr->err ? t->hctr->err : VD_OK;
+}
+
+int vd_duplicates(vd_tree* t, int64_t* pairs, int64_t cap, int64_t* n) {
+  if (ready(t) || !n) return VD_ERR_ARG;
+  int rc = sync_counters(t);
+  if (rc) return rc;
+  const int64_t m = std::min<int64_t>(t->hctr->ndup, t->T.cap_dups);
+  *n = m;
+  if (!pairs) return VD_OK;
+  if (cap < m) return VD_ERR_ARG;
+  std::vector<int2> h(m);
+  if (m) {
+    cudaMemcpyAsync(h.data(), t->T.dups, sizeof(int2) * m, cudaMemcpyDeviceToHost, t->stream);
+    if (cudaStreamSynchronize(t->stream) != cudaSuccess) return VD_ERR_CUDA;
+  }
+  std::sort(h.begin(), h.end(), [](const int2& a, const int2& b) { return a.x < b.x; });
+  for (int64_t i = 0; i < m; ++i) {
+    pairs[2 * i] = h[i].x - t->ns;
+    pairs[2 * i + 1] = h[i].y - t->ns;
+  }
+  return VD_OK;
+}
+
+int vd_get_stats(vd_tree* t, vd_stats* s) {
+  if (ready(t) || !s) return VD_ERR_ARG;
+  int rc = sync_counters(t);
+  if (rc) return rc;
+  const Counters& h = *t->hctr;
+  s->rounds = t->round;
+  s->inserted = h.ninserted;
+  s->duplicates = h.ndup;
+  s->live_simplices = 1 + (int64_t)h.created - (int64_t)h.killed;
+  s->slots = h.nsimp;
+  s->created = (int64_t)h.created;
+  s->killed = (int64_t)h.killed;
+  s->max_cavity = h.max_cav;
+  s->max_facets = h.max_fac;
+  s->pred_f32 = (int64_t)h.tally[0];
+  s->pred_f64 = (int64_t)h.tally[1];
+  s->pred_exact = (int64_t)h.tally[2];
+  s->pred_sos = (int64_t)h.tally[3];
+  s->walk_steps = (int64_t)h.walk;
+  s->cavity_tests = (int64_t)h.cavity_tests;
+  s->deferred_overflow = h.overflow;
+  s->deferred_pool = h.pool_overflow;
+  s->candidates = (int64_t)h.candidates;
+  s->searched = (int64_t)h.searched;
+  for (int p = 0; p < 3; ++p) s->won_pass[p] = (int64_t)h.won[p];
+  for (int p = 3; p < vd::kPassesMax; ++p) s->won_pass[2] += (int64_t)h.won[p];
+  s->spilled = (int64_t)h.spilled;
+  return VD_OK;
+}
+
+int vd_delaunay(int dim, const double* pts, int64_t n, uint64_t seed, int64_t* uv, int64_t cap,
+                int64_t* n_edges) {
+  int st = 0;
+  vd_tree* t = vd_tree_new(dim, pts, n, &st);
+  if (!t) return VD_ERR_NOMEM;
+  if (st) {
+    vd_tree_free(t);
+    return st;
+  }
+  int rc = vd_insert_points(t, pts, n, seed);
+  if (rc && rc != VD_ERR_DUPLICATE) {
+    vd_tree_free(t);
+    return rc;
+  }
+  int rc2 = vd_edges(t, uv, cap, n_edges);
+  vd_tree_free(t);
+  return rc2 ? rc2 : rc;
+}
+
+int vd_set_profiling(vd_tree* t, int on) {
+  if (ready(t)) return VD_ERR_ARG;
+  t->prof = on != 0;
+  for (int k = 0; k < vd::KT_COUNT; ++k) {
+    t->kms[k] = 0.0;
+    t->kcnt[k] = 0;
+  }
+  return VD_OK;
+}
+
+int vd_profile(vd_tree* t, double* ms, int64_t* launches, int cap, int* n) {
+  if (ready(t) || !n) return VD_ERR_ARG;
+  *n = vd::KT_COUNT;
+  if (!ms && !launches) return VD_OK;
+  if (cap < *n) return VD_ERR_ARG;
+  for (int k = 0; k < vd::KT_COUNT; ++k) {
+    if (ms) ms[k] = t->kms[k];
+    if (launches) launches[k] = t->kcnt[k];
+  }
+  return VD_OK;
+}
+
+const char* vd_profile_name(int i) {
+  if (i >= 0 && i < vd::KT_COUNT) return vd::kKernelTypeNames[i];
+  return "";
+}
+
+int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth) {
+  if (ready(t) || first_prefix < 1 || !(growth >= 1.5)) return VD_ERR_ARG;
+  t->first_prefix = first_prefix;
+  t->growth = growth;
+  return VD_OK;
+}
+
+int vd_set_tuning(vd_tree* t, int passes, int thin) {
+  if (ready(t) || passes < 1 || passes > vd::kPassesMax || thin < 1 || thin > 2) return VD_ERR_ARG;
+  t->tuning.passes = passes;
+  t->tuning.thin = thin;
+  return VD_OK;
+}
+
+int vd_set_trace(vd_tree* t, int on) {
+  if (ready(t)) return VD_ERR_ARG;
+  t->trace = on != 0;
+  t->trace_rows.clear();
+  return VD_OK;
+}
+
+int vd_trace(vd_tree* t, int64_t* rows, int64_t cap, int64_t* n) {
+  if (ready(t) || !n) return VD_ERR_ARG;
+  *n = (int64_t)t->trace_rows.size() / 8;
+  if (!rows) return VD_OK;
+  if (cap < *n) return VD_ERR_ARG;
+  std::copy(t->trace_rows.begin(), t->trace_rows.end(), rows);
+  return VD_OK;
+}
+
+int vd_locate(vd_tree* t, const double* p, int64_t* out, int64_t cap, int64_t* n) {
+  (void)t;
+  (void)p;
+  (void)out;
+  (void)cap;
+  (void)n;
+  return VD_ERR_ARG;  // implemented in a later revision of the query API
+}
+
+}  // extern "C"

@@ -1,0 +1,206 @@
+// Device-side data layout of a Delaunay tree on one GPU.
+//
+// The reference keeps simplices in a DashMap<usize, Simplex> with a
+// Vec<usize> of neighbours each and a kd-tree of vertices
+// (src/delaunay_tree.rs:10-30).  Here everything is a flat, device-resident
+// pool addressed by 32-bit indices:
+//
+//   pts[v]        vertex v: (x, y, z | 0, pad) f64, 32 B, one sector per gather;
+//                 ids 0..D are the super-simplex vertices, D+1+i is input point i
+//   simp[s]       simplex slot s: v[0..D] vertex ids (positively oriented),
+//                 n[f] = (neighbour << 2) | face-in-neighbour across the face
+//                 opposite v[f], or -1 on the super-simplex hull; a dead slot
+//                 has v[0] = -1 and n[0] pointing at a simplex of the star that
+//                 replaced it.  32 B = one sector.
+//   vote[s]       epoch|priority of the lowest-priority uninserted point inside s
+//   thin[s]       epoch|priority of the lowest candidate whose simplex is s or
+//                 a face neighbour of s (cheap pre-selection before any search)
+//   claim_c[s]    epoch|priority of the lowest candidate whose cavity holds s
+//   claim_n[s]    epoch|priority of the lowest candidate that rewrites a face of s
+//   killed[s]     (round, vertex) of the insertion that removed s
+//   touched[s]    round in which an insertion repointed a face of s
+//
+// Epoch-tagged 64-bit keys ((2^32 - 1 - round) << 32 | priority) make stale
+// values from earlier rounds compare larger, so none of these arrays is ever
+// cleared between rounds.
+#pragma once
+#include <stdint.h>
+
+#include "vd_predicates.cuh"
+
+namespace vd {
+
+struct alignas(32) Simplex {
+  int v[4];
+  int n[4];
+};
+
+// Per-round statuses of a candidate.
+enum : int { ST_OK = 0, ST_DUP = 1, ST_OVERFLOW = 2, ST_POOL = 3, ST_LOST = 4, ST_DONE = 5 };
+
+// Resolution passes per round (independent-set refinement), see vd_build.cu.
+constexpr int kPassesMax = 6;
+
+// Error codes (mirrored by the C ABI's vd_status).
+enum : int {
+  E_OK = 0,
+  E_ARG = 1,
+  E_CUDA = 2,
+  E_NOMEM = 3,
+  E_DUPLICATE = 4,
+  E_NONFINITE = 5,
+  E_OUTSIDE = 6,
+  E_PRECISION = 7,
+  E_ROUND_LIMIT = 8,
+  E_CAVITY = 9,
+  E_WALK = 10,
+  E_INTERNAL = 11,
+  E_DEGENERATE = 12,
+  E_RANGE = 13,
+};
+
+struct Counters {
+  int nact[2];        // active (uninserted) points, by round parity
+  int ncand;          // candidates of the current round
+  int pool_used;      // ints of the cavity pool used in the current round
+  int nsimp;          // simplex slots handed out (high-water mark)
+  int wasted;         // slots reserved by allocations that did not fit
+  int err;            // first error code
+  int ndup;           // duplicates dropped
+  int overflow;       // candidates deferred: cavity larger than a warp holds
+  int pool_overflow;  // candidates deferred: cavity pool full
+  int simp_overflow;  // winners deferred: simplex pool full
+  int ninserted;      // vertices inserted (total)
+  int winners;        // winners (total)
+  int max_cav, max_fac;
+  int holes;          // dead slots left when a cavity had more simplices than facets
+  unsigned long long created;  // simplices created (total)
+  unsigned long long killed;   // simplices removed (total)
+  unsigned long long tally[4]; // predicate decisions: f32, f64, exact, sos
+  unsigned long long walk;     // relocation walk steps
+  unsigned long long cavity_tests;  // conflict tests in cavity searches
+  unsigned long long candidates;    // nominated points (all rounds)
+  unsigned long long searched;      // candidates that passed the thinning claim
+  unsigned long long won[kPassesMax];  // winners per resolution pass
+  unsigned long long spilled;       // searches that used the pool spill path
+};
+
+// Insertion proceeds in priority prefixes (see vd_capi.cu); at most this many.
+constexpr int kMaxPrefixes = 48;
+
+struct DevTree {
+  vdp::VPt* pts;
+  vdp::FPt* ptf;      // the same coordinates split into f32 hi/lo pairs
+  Simplex* simp;
+  unsigned long long* vote;
+  unsigned long long* thin;
+  unsigned long long* claim_c;
+  unsigned long long* claim_n;
+  int2* killed;
+  int* touched;
+  int4* act[2];   // (vid, loc, priority, 0)
+  int4* cand;     // (vid, loc, priority, active slot)
+  int4* cinfo;    // (ncav, nfac, pool offset, status)
+  int* pool;
+  int2* dups;     // (dropped vid, vid it equals)
+  Counters* ctr;
+  int2* wchunk;       // per-warp fresh-slot chunk (base, left) of k_check
+  int cap_wchunk;
+  int* hint;          // location hints, levels 0..hint_levels (see vd_build.cu)
+  int hint_levels;
+  double gorg[3];     // hint grid origin and 1 / extent
+  double gscale;
+  int cap_simp;
+  int cap_verts;
+  int cap_pool;
+  int cap_cand;
+  int cap_dups;
+};
+
+__host__ __device__ inline unsigned long long epoch(int round) {
+  return (unsigned long long)(0xFFFFFFFFu - (unsigned)round) << 32;
+}
+// Claim keys of resolution pass p of round r (later passes compare lower).
+__host__ __device__ inline unsigned long long pass_epoch(int round, int pass) {
+  return epoch(8 * round + pass);
+}
+
+// Insertion priority: a bijective mix of the 32-bit vertex id and the seed,
+// so priorities are distinct and form a seeded random order.
+__host__ __device__ inline uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+__host__ __device__ inline uint32_t priority(uint32_t vid, uint64_t seed) {
+  uint32_t x = vid ^ (uint32_t)seed;
+  x = mix32(x);
+  x ^= (uint32_t)(seed >> 32);
+  return mix32(x);
+}
+
+#if defined(__CUDACC__)
+__device__ inline void set_error(Counters* c, int code) { atomicCAS(&c->err, 0, code); }
+// Index guards: a corrupted structure must turn into an error status, never
+// into an out-of-bounds access.
+__device__ inline bool bad_simp(const DevTree& T, int s) { return (unsigned)s >= (unsigned)T.cap_simp; }
+__device__ inline bool bad_vert(const DevTree& T, int v) { return (unsigned)v >= (unsigned)T.cap_verts; }
+#endif
+
+// Host-side launchers (vd_build.cu, vd_edges.cu, vd_check.cu).
+struct Launch {
+  int blocks;      // persistent grid size for thread-per-item kernels
+  int warps;       // persistent warp count for warp-per-item kernels (multiple of 4)
+  cudaStream_t stream;
+};
+
+void launch_upload(const DevTree& T, const Launch& L, int dim, const double* d_xyz, int64_t n,
+                   int base_vid, const int* super_order);
+void launch_prefix_hist(const Launch& L, int64_t n, int base_vid, uint64_t seed,
+                        const unsigned long long* thr, int nthr, int* d_counts);
+void launch_activate(const DevTree& T, const Launch& L, int dim, int64_t n, int base_vid, uint64_t seed,
+                     unsigned long long lo, unsigned long long hi, int round);
+// Runtime tuning of a round: resolution passes (1..kPassesMax) and the
+// thinning radius (1: face neighbours, 2: also their neighbours).
+struct Tuning {
+  int passes;
+  int thin;
+};
+// Kernel types for profiling.
+enum { KT_PICK, KT_CAVITY, KT_CHECK, KT_RECLAIM, KT_RELOCATE, KT_ACTIVATE, KT_EDGES, KT_COUNT };
+extern const char* const kKernelTypeNames[KT_COUNT];
+// Event log of one round: ev[0] before the first kernel, ev[i + 1] after
+// kernel i, whose type is type[i].
+struct Prof {
+  static constexpr int kMax = 4 + 2 * kPassesMax;
+  cudaEvent_t ev[kMax + 1];
+  int type[kMax];
+  int n;
+};
+void launch_round(const DevTree& T, const Launch& L, int dim, int round, const Tuning& tu, Prof* pf);
+
+// Edges: counts / offsets / segment buffers are caller-provided device arrays.
+struct EdgeScratch {
+  int* cnt;        // n_in + 1
+  int* off;        // n_in + 1
+  int* buf;        // capacity cap_buf
+  int* ucnt;       // n_in + 1
+  int* uoff;       // n_in + 1
+  int* big;        // list of vertices with long segments, capacity n_in
+  int* nbig;       // 1 int
+  int* scan_tmp;   // scan scratch (see scan_scratch_ints)
+  int64_t cap_buf;
+};
+int64_t scan_scratch_ints(int64_t n);
+void launch_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_in,
+                  const EdgeScratch& S, uint2* d_out);
+
+// Validator: out[0..5] = non-positive, asymmetric, not Delaunay (exact),
+// not perturbed-Delaunay, hull facets, facets checked.
+void launch_check(const DevTree& T, const Launch& L, int dim, int nsimp,
+                  unsigned long long* d_out);
+
+}  // namespace vd
