@@ -151,9 +151,9 @@ int vd_set_profiling(vd_tree* t, int on);
  * priority prefixes of `first_prefix` points, then growing by `growth` (>= 1.5)
  * per prefix.  Defaults 64 and 4. */
 int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth);
-/* Round tuning: resolution passes per round (1..6, default 3) and the
- * thinning radius (1 = a nominee must hold its simplex and face neighbours,
- * 2 = and no lower nominee two faces away; default 1). */
+/* Round tuning: resolution passes per round (1..6) and the thinning radius
+ * (1 = a nominee must hold its simplex and face neighbours, 2 = and no lower
+ * nominee two faces away).  Defaults: 3D 2 passes / radius 2, 2D 3 / 1. */
 int vd_set_tuning(vd_tree* t, int passes, int thin);
 int vd_profile(vd_tree* t, double* ms, int64_t* launches, int cap, int* n);
 const char* vd_profile_name(int i);

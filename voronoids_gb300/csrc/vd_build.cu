@@ -289,7 +289,10 @@ __global__ void k_activate(DevTree T, long long n, int base, unsigned long long 
 // ---------------------------------------------------------------------------
 __global__ void k_pick(DevTree T, int round) {
   const int par = round & 1;
-  if (blockIdx.x == 0 && threadIdx.x == 0) T.ctr->nact[par ^ 1] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    T.ctr->nact[par ^ 1] = 0;
+    for (int k = 0; k < kStages; ++k) T.ctr->nwl[k] = 0;
+  }
   const int n = T.ctr->nact[par];
   const unsigned long long ep = epoch(round);
   unsigned long long ncand = 0;
@@ -456,27 +459,6 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
   __syncwarp();
 }
 
-template <int D>
-struct WarpCav {
-  WarpCtl ctl;
-  int cav[Cap<D>::MAXC];
-  int4 cv[Cap<D>::MAXC];
-  int4 cn[Cap<D>::MAXC];
-  int hkey[Cap<D>::HS];
-  int fr[6 * Cap<D>::MAXF];
-};
-
-// Claims of a candidate for one resolution pass: its cavity in claim_c, every
-// outer neighbour in claim_n.  P = cavity ids, F = facet records.
-__device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int ncav, const int* F,
-                                             int nfac, unsigned long long key, int lane) {
-  for (int i = lane; i < ncav; i += 32) atomicMin(T.claim_c + P[i], key);
-  for (int j = lane; j < nfac; j += 32) {
-    const int o = F[6 * j + 4];
-    if (o >= 0 && !bad_simp(T, o >> 2)) atomicMin(T.claim_n + (o >> 2), key);
-  }
-}
-
 // Thinning test of one nominee (one thread): it must hold the thinning claim
 // on its simplex and on every face neighbour; with `thin` >= 2 no lower
 // nominee may claim a simplex two faces away either.
@@ -504,32 +486,19 @@ __device__ bool thin_lost1(const DevTree& T, int home, int4 n0, unsigned long lo
   return false;
 }
 
+// Per nominee (one thread): duplicate test against the vertices of its
+// simplex and the thinning test; survivors go to work list stage 0.
 template <int D>
-__global__ void __launch_bounds__(128) k_cavity(DevTree T, int round, int thin) {
-  constexpr int NV = D + 1, MAXC = Cap<D>::MAXC, MAXF = Cap<D>::MAXF, HS = Cap<D>::HS;
-  __shared__ WarpCav<D> smem[4];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  WarpCav<D>& W = smem[wib];
+__global__ void k_thin(DevTree T, int round, int thin) {
+  constexpr int NV = D + 1;
   const int nc = min(T.ctr->ncand, T.cap_cand);
   const unsigned long long ep = epoch(round);
-  const unsigned long long pe = pass_epoch(round, 0);
   const int par = round & 1;
-  vdp::Tally tl = {0, 0, 0, 0};
-  int perr = 0;
-  unsigned long long ntests = 0, nsearched = 0, nspill = 0;
-  int mcav = 0, mfac = 0;
-  // pool space is taken in per-warp chunks (one atomic per chunk, not per
-  // candidate); what a warp leaves unused is dropped with the round's pool
-  const int pchunk = max(256, min(8192, T.cap_pool / (gridDim.x * 16)));
-  int pbase = 0, pleft = 0;
-  const CavStore fast{W.cav, W.cv, W.cn, W.hkey, W.fr, MAXC, MAXF, HS};
-  // Warps take strips of 32 nominees: duplicate and thinning tests run one
-  // nominee per lane, then the warp searches the survivors one by one.
-  for (int base = (blockIdx.x * 4 + wib) * 32; base < nc; base += gridDim.x * 4 * 32) {
-    const int cl = base + lane;
+  for (int b = blockIdx.x * blockDim.x; b < nc; b += gridDim.x * blockDim.x) {
+    const int c = b + threadIdx.x;
     bool survive = false;
-    if (cl < nc) {
-      const int4 e = T.cand[cl];
+    if (c < nc) {
+      const int4 e = T.cand[c];
       int4 v, n;
       load_simplex(T, e.y, v, n);
       const vdp::VPt q = load_pt(T, e.x);
@@ -542,18 +511,59 @@ __global__ void __launch_bounds__(128) k_cavity(DevTree T, int round, int thin) 
         T.act[par][e.w].x = -1;
         const int k = atomicAdd(&T.ctr->ndup, 1);
         if (k < T.cap_dups) T.dups[k] = make_int2(e.x, dup);
-        T.cinfo[cl] = make_int4(0, 0, 0, ST_DUP);
+        T.cinfo[c] = make_int4(0, 0, 0, ST_DUP);
       } else if (thin_lost1<D>(T, e.y, n, ep | (unsigned)e.z, thin)) {
-        T.cinfo[cl] = make_int4(0, 0, 0, ST_LOST);
+        T.cinfo[c] = make_int4(0, 0, 0, ST_LOST);
       } else {
         survive = true;
       }
     }
-    unsigned todo = __ballot_sync(FULL, survive);
-    while (todo) {
-    const int src = __ffs(todo) - 1;
-    todo &= todo - 1;
-    const int c = base + src;
+    const int k = warp_append(&T.ctr->nwl[0], survive);
+    if (survive) T.wl[0][k] = c;
+  }
+}
+
+template <int D>
+struct WarpCav {
+  WarpCtl ctl;
+  int cav[Cap<D>::MAXC];
+  int4 cv[Cap<D>::MAXC];
+  int4 cn[Cap<D>::MAXC];
+  int hkey[Cap<D>::HS];
+  int fr[6 * Cap<D>::MAXF];
+};
+
+// Claims of a candidate for one resolution pass: its cavity in claim_c, every
+// outer neighbour in claim_n.  P = cavity ids, F = facet records.
+__device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int ncav, const int* F,
+                                             int nfac, unsigned long long key, int lane) {
+  for (int i = lane; i < ncav; i += 32) atomicMin(T.claim_c + P[i], key);
+  for (int j = lane; j < nfac; j += 32) {
+    const int o = F[6 * j + 4];
+    if (o >= 0 && !bad_simp(T, o >> 2)) atomicMin(T.claim_n + (o >> 2), key);
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_cavity(DevTree T, int round) {
+  constexpr int MAXC = Cap<D>::MAXC, MAXF = Cap<D>::MAXF, HS = Cap<D>::HS;
+  __shared__ WarpCav<D> smem[4];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WarpCav<D>& W = smem[wib];
+  const unsigned long long pe = pass_epoch(round, 0);
+  vdp::Tally tl = {0, 0, 0, 0};
+  int perr = 0;
+  unsigned long long ntests = 0, nsearched = 0, nspill = 0;
+  int mcav = 0, mfac = 0;
+  // pool space is taken in per-warp chunks (one atomic per chunk, not per
+  // candidate); what a warp leaves unused is dropped with the round's pool
+  const int pchunk = max(256, min(8192, T.cap_pool / (gridDim.x * 16)));
+  int pbase = 0, pleft = 0;
+  const CavStore fast{W.cav, W.cv, W.cn, W.hkey, W.fr, MAXC, MAXF, HS};
+  const int nw = gridDim.x * 4;
+  const int nsurv = T.ctr->nwl[0];
+  for (int it = blockIdx.x * 4 + wib; it < nsurv; it += nw) {
+    const int c = T.wl[0][it];
     const int4 cd = T.cand[c];
     const vdp::VPt q = load_pt(T, cd.x);
     const vdp::FPt fq = load_fpt(T, cd.x);
@@ -629,7 +639,6 @@ __global__ void __launch_bounds__(128) k_cavity(DevTree T, int round, int thin) 
     mcav = max(mcav, ncav);
     mfac = max(mfac, nfac);
     __syncwarp();
-    }
   }
   if (perr) set_error(T.ctr, E_PRECISION);
   flush_tally(T.ctr, tl, ntests, 0);
@@ -657,15 +666,15 @@ __device__ __forceinline__ void cand_lists(const DevTree& T, const int4& info, i
 
 template <int D>
 struct WarpCommit {
+  static constexpr int HR = D == 3 ? 512 : 256;  // ridge table slots (> 2x ridges)
+  unsigned long long rk[HR];   // ridge key (r0 << 32 | r1)
+  int ra[HR], rb[HR];          // the two half-ridges (facet << 2 | face)
   int fr[6 * Cap<D>::MAXF];
   int id[Cap<D>::MAXF];
   int first[Cap<D>::MAXC];     // first facet index of each cavity simplex
   int freeslot[Cap<D>::MAXC];  // cavity slots without an own facet
 };
 
-__device__ __forceinline__ bool has4(const int* a, int x) {
-  return a[0] == x || a[1] == x || a[2] == x || a[3] == x;
-}
 
 // Ridge of face g of new simplex r (vertices r[0..3], new vertex at qf): the
 // vertices other than r[g] and the new vertex, smaller first (2D: one vertex).
@@ -696,14 +705,38 @@ __device__ __forceinline__ void emit_simplex(const DevTree& T, const int* r, int
   }
 }
 
-// Star of one winner, small case: ridge partners found by scanning the facet
-// records (shared memory, at most Cap::MAXF of them).
+// Star of one winner, small case: the half-ridges of all new simplices go
+// into a shared-memory table keyed by the ridge's vertices; each ridge has
+// exactly two halves, which are each other's neighbours.
 template <int D>
-__device__ void write_star(const DevTree& T, const int* FR, const int* ID, int nfac, int qv, int round,
-                           int lane) {
-  constexpr int NV = D + 1;
+__device__ void write_star(const DevTree& T, WarpCommit<D>& W, int nfac, int qv, int round, int lane) {
+  constexpr int NV = D + 1, HR = WarpCommit<D>::HR;
+  const unsigned long long EMPTY = ~0ull;
+  for (int i = lane; i < HR; i += 32) {
+    W.rk[i] = EMPTY;
+    W.ra[i] = -1;
+  }
+  __syncwarp();
+  for (int it = lane; it < nfac * NV; it += 32) {
+    const int j = it / NV, g = it - j * NV;
+    const int* r = W.fr + 6 * j;
+    const int qf = r[5] & 3;
+    if (g == qf) continue;
+    int r0, r1;
+    ridge_of<D>(r, g, qf, r0, r1);
+    const unsigned long long key = ((unsigned long long)(unsigned)r0 << 32) | (unsigned)r1;
+    unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> 40) & (HR - 1);
+    for (int probe = 0; probe < HR; ++probe, h = (h + 1) & (HR - 1)) {
+      const unsigned long long old = atomicCAS(&W.rk[h], EMPTY, key);
+      if (old == EMPTY || old == key) {
+        if (atomicCAS(&W.ra[h], -1, (j << 2) | g) != -1) W.rb[h] = (j << 2) | g;
+        break;
+      }
+    }
+  }
+  __syncwarp();
   for (int j = lane; j < nfac; j += 32) {
-    const int* r = FR + 6 * j;
+    const int* r = W.fr + 6 * j;
     const int qf = r[5] & 3;
     int4 nn = make_int4(-1, -1, -1, -1);
     nn = set4(nn, qf, r[4]);
@@ -711,26 +744,32 @@ __device__ void write_star(const DevTree& T, const int* FR, const int* ID, int n
       if (g == qf) continue;
       int r0, r1;
       ridge_of<D>(r, g, qf, r0, r1);
-      int found = -1, pos = -1;
-      for (int m = 0; m < nfac; ++m) {
-        if (m == j) continue;
-        const int* w = FR + 6 * m;
-        if (!has4(w, r0)) continue;
-        if (D == 3 && !has4(w, r1)) continue;
-        found = m;
-        for (int i = 0; i < NV; ++i) {
-          const int x = w[i];
-          if (x != qv && x != r0 && x != r1) pos = i;
+      const unsigned long long key = ((unsigned long long)(unsigned)r0 << 32) | (unsigned)r1;
+      unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> 40) & (HR - 1);
+      int other = -1;
+      for (int probe = 0; probe < HR; ++probe, h = (h + 1) & (HR - 1)) {
+        const unsigned long long k2 = W.rk[h];
+        if (k2 == EMPTY) break;
+        if (k2 == key) {
+          other = W.ra[h] == ((j << 2) | g) ? W.rb[h] : W.ra[h];
+          break;
         }
-        break;
       }
-      if (found < 0 || pos < 0) {
+      const int m = other >> 2;
+      int pos = -1;
+      if (other >= 0 && m < nfac) {
+        const int* w = W.fr + 6 * m;
+        const int qm = w[5] & 3;
+        for (int i = 0; i < NV; ++i)
+          if (i != qm && w[i] != r0 && w[i] != r1) pos = i;
+      }
+      if (pos < 0) {
         set_error(T.ctr, E_INTERNAL);
         continue;
       }
-      nn = set4(nn, g, (ID[found] << 2) | pos);
+      nn = set4(nn, g, (W.id[m] << 2) | pos);
     }
-    emit_simplex(T, r, ID[j], nn, round);
+    emit_simplex(T, r, W.id[j], nn, round);
   }
 }
 
@@ -821,10 +860,11 @@ __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, i
 // k usually finds itself in (or next to) the simplex now in k's slot.
 template <int D>
 __global__ void __launch_bounds__(128) k_check(DevTree T, int round, int pass, int last) {
+  const int sin = 2 * pass, sout = 2 * pass + 1;
   constexpr int MAXF = Cap<D>::MAXF, MAXC = Cap<D>::MAXC;
-  __shared__ WarpCommit<D> smem[4];
+  extern __shared__ __align__(16) unsigned char dsm[];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  WarpCommit<D>& W = smem[wib];
+  WarpCommit<D>& W = reinterpret_cast<WarpCommit<D>*>(dsm)[wib];
   const int nc = min(T.ctr->ncand, T.cap_cand);
   const unsigned long long pe = pass_epoch(round, pass);
   const int par = round & 1;
@@ -833,13 +873,12 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int round, int pass, i
   // fresh simplex slots come from a per-warp chunk kept across launches
   const int gw = blockIdx.x * 4 + wib;
   int2 chunk = gw < T.cap_wchunk ? T.wchunk[gw] : make_int2(0, 0);
-  for (int sb = (blockIdx.x * 4 + wib) * 32; sb < nc; sb += gridDim.x * 4 * 32) {
-    const bool pend = sb + lane < nc && T.cinfo[sb + lane].w == ST_OK;
-    unsigned todo = __ballot_sync(FULL, pend);
-    while (todo) {
-    const int c = sb + __ffs(todo) - 1;
-    todo &= todo - 1;
+  const int nw = gridDim.x * 4;
+  const int nin = T.ctr->nwl[sin];
+  for (int it = blockIdx.x * 4 + wib; it < nin; it += nw) {
+    const int c = T.wl[sin & 1][it];
     const int4 info = T.cinfo[c];
+    if (info.w != ST_OK) continue;
     const int4 cd = T.cand[c];
     const unsigned long long key = pe | (unsigned)cd.z;
     int *P, *F, ncav, nfac;
@@ -860,7 +899,14 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int round, int pass, i
       ok = ok && !bad_simp(T, o >> 2) && T.claim_c[o >> 2] > key;
     }
     if (!__all_sync(FULL, ok)) {
-      if (last && lane == 0) T.cinfo[c].w = ST_LOST;
+      if (lane == 0) {
+        if (last) {
+          T.cinfo[c].w = ST_LOST;
+        } else {
+          const int k = atomicAdd(&T.ctr->nwl[sout], 1);
+          T.wl[sout & 1][k] = c;
+        }
+      }
       continue;
     }
     const int fresh = max(0, nfac - ncav);
@@ -926,7 +972,7 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int round, int pass, i
       // leftover cavity slots become holes pointing into the star
       for (int t = nsec + lane; t < nfree; t += 32)
         store_simplex(T, W.freeslot[t], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
-      write_star<D>(T, W.fr, W.id, nfac, cd.x, round, lane);
+      write_star<D>(T, W, nfac, cd.x, round, lane);
     } else {
       // large star (spilled search): plain slot assignment, ids in the
       // stretch's vertex-list area (free after the search), ridge table in
@@ -949,7 +995,6 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int round, int pass, i
     nkilled += ncav;
     nholes += max(0, ncav - nfac);
     __syncwarp();
-    }
   }
   if (lane == 0) {
     if (gw < T.cap_wchunk) T.wchunk[gw] = chunk;
@@ -970,16 +1015,16 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int round, int pass, i
 // again with this pass's key (smaller than every earlier key of the round).
 template <int D>
 __global__ void __launch_bounds__(128) k_reclaim(DevTree T, int round, int pass) {
+  const int sin = 2 * pass - 1, sout = 2 * pass;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nc = min(T.ctr->ncand, T.cap_cand);
   const unsigned long long pe = pass_epoch(round, pass);
-  for (int sb = (blockIdx.x * 4 + wib) * 32; sb < nc; sb += gridDim.x * 4 * 32) {
-    const bool pend = sb + lane < nc && T.cinfo[sb + lane].w == ST_OK;
-    unsigned todo = __ballot_sync(FULL, pend);
-    while (todo) {
-    const int c = sb + __ffs(todo) - 1;
-    todo &= todo - 1;
+  const int nw = gridDim.x * 4;
+  const int nin = T.ctr->nwl[sin];
+  for (int it = blockIdx.x * 4 + wib; it < nin; it += nw) {
+    const int c = T.wl[sin & 1][it];
     const int4 info = T.cinfo[c];
+    if (info.w != ST_OK) continue;
     const int4 cd = T.cand[c];
     int *P, *F, ncav, nfac;
     bool big;
@@ -998,6 +1043,9 @@ __global__ void __launch_bounds__(128) k_reclaim(DevTree T, int round, int pass)
       continue;
     }
     claim_region(T, P, ncav, F, nfac, pe | (unsigned)cd.z, lane);
+    if (lane == 0) {
+      const int k = atomicAdd(&T.ctr->nwl[sout], 1);
+      T.wl[sout & 1][k] = c;
     }
   }
 }
@@ -1080,6 +1128,11 @@ __global__ void k_relocate(DevTree T, int round) {
 
 template <int D>
 void round_impl(const DevTree& T, const Launch& L, int round, const Tuning& tu, Prof* pf) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_check<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * (int)sizeof(WarpCommit<D>));
+    attr = true;
+  }
   auto mark = [&](int type) {
     if (pf && pf->n < Prof::kMax) {
       cudaEventRecord(pf->ev[pf->n + 1], L.stream);
@@ -1089,14 +1142,16 @@ void round_impl(const DevTree& T, const Launch& L, int round, const Tuning& tu, 
   if (pf && pf->n == 0) cudaEventRecord(pf->ev[0], L.stream);
   k_pick<<<L.blocks, 256, 0, L.stream>>>(T, round);
   mark(KT_PICK);
-  k_cavity<D><<<L.warps / 4, 128, 0, L.stream>>>(T, round, tu.thin);
+  k_thin<D><<<L.blocks, 256, 0, L.stream>>>(T, round, tu.thin);
+  mark(KT_THIN);
+  k_cavity<D><<<L.warps / 4, 128, 0, L.stream>>>(T, round);
   mark(KT_CAVITY);
   for (int p = 0; p < tu.passes; ++p) {
     if (p > 0) {
       k_reclaim<D><<<L.warps / 4, 128, 0, L.stream>>>(T, round, p);
       mark(KT_RECLAIM);
     }
-    k_check<D><<<L.warps / 4, 128, 0, L.stream>>>(T, round, p, p == tu.passes - 1);
+    k_check<D><<<L.warps / 4, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, round, p, p == tu.passes - 1);
     mark(KT_CHECK);
   }
   k_relocate<D><<<L.blocks, 256, 0, L.stream>>>(T, round);
@@ -1137,7 +1192,7 @@ void launch_round(const DevTree& T, const Launch& L, int dim, int round, const T
     round_impl<2>(T, L, round, tu, pf);
 }
 
-const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_cavity",   "k_check", "k_reclaim",
-                                                "k_relocate", "k_activate", "edges"};
+const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_thin",     "k_cavity", "k_check",
+                                                "k_reclaim",  "k_relocate", "k_activate", "edges"};
 
 }  // namespace vd

@@ -143,7 +143,7 @@ struct vd_tree {
   std::vector<vd::Prof> profs;   // one event log per round of a chunk
   double kms[vd::KT_COUNT] = {};
   int64_t kcnt[vd::KT_COUNT] = {};
-  vd::Tuning tuning = {3, 1};
+  vd::Tuning tuning = {2, 2};
   // per-round trace (diagnostics; syncs after every round)
   bool trace = false;
   std::vector<int64_t> trace_rows;
@@ -269,8 +269,10 @@ int ensure_points(vd_tree* t, int64_t n_new) {
     dfree(t->T.act[1]);
     dfree(t->T.cand);
     dfree(t->T.cinfo);
+    dfree(t->T.wl[0]);
+    dfree(t->T.wl[1]);
     if (dalloc(&t->T.act[0], c) || dalloc(&t->T.act[1], c) || dalloc(&t->T.cand, c) ||
-        dalloc(&t->T.cinfo, c))
+        dalloc(&t->T.cinfo, c) || dalloc(&t->T.wl[0], c) || dalloc(&t->T.wl[1], c))
       return vd::E_NOMEM;
     t->cap_act = c;
     t->T.cap_cand = (int)c;
@@ -310,6 +312,8 @@ void release(vd_tree* t) {
   dfree(t->T.act[1]);
   dfree(t->T.cand);
   dfree(t->T.cinfo);
+  dfree(t->T.wl[0]);
+  dfree(t->T.wl[1]);
   dfree(t->T.pool);
   dfree(t->T.dups);
   dfree(t->T.ctr);
@@ -350,6 +354,7 @@ int init_tree(vd_tree* t, int dim, const double* pts, int64_t n, void* stream) {
   }
   t->dim = dim;
   t->ns = dim + 1;
+  t->tuning = dim == 3 ? vd::Tuning{2, 2} : vd::Tuning{3, 1};
   ref_super_vertices(dim, pts, n, t->sup, &t->R);
   if (!(t->R > 0.0) || !isfinite(t->R)) return vd::E_DEGENERATE;
   for (int i = 0; i < t->ns; ++i)

@@ -40,6 +40,9 @@ enum : int { ST_OK = 0, ST_DUP = 1, ST_OVERFLOW = 2, ST_POOL = 3, ST_LOST = 4, S
 
 // Resolution passes per round (independent-set refinement), see vd_build.cu.
 constexpr int kPassesMax = 6;
+// Work-list stages of a round: 0 = searched nominees, then per pass the
+// losers (odd) and the re-claimers (even).
+constexpr int kStages = 2 * kPassesMax;
 
 // Error codes (mirrored by the C ABI's vd_status).
 enum : int {
@@ -83,6 +86,7 @@ struct Counters {
   unsigned long long searched;      // candidates that passed the thinning claim
   unsigned long long won[kPassesMax];  // winners per resolution pass
   unsigned long long spilled;       // searches that used the pool spill path
+  int nwl[kStages];                 // work-list lengths of the current round
 };
 
 // Insertion proceeds in priority prefixes (see vd_capi.cu); at most this many.
@@ -101,6 +105,7 @@ struct DevTree {
   int4* act[2];   // (vid, loc, priority, 0)
   int4* cand;     // (vid, loc, priority, active slot)
   int4* cinfo;    // (ncav, nfac, pool offset, status)
+  int* wl[2];     // work lists (candidate indices), stage s in wl[s & 1]
   int* pool;
   int2* dups;     // (dropped vid, vid it equals)
   Counters* ctr;
@@ -170,12 +175,12 @@ struct Tuning {
   int thin;
 };
 // Kernel types for profiling.
-enum { KT_PICK, KT_CAVITY, KT_CHECK, KT_RECLAIM, KT_RELOCATE, KT_ACTIVATE, KT_EDGES, KT_COUNT };
+enum { KT_PICK, KT_THIN, KT_CAVITY, KT_CHECK, KT_RECLAIM, KT_RELOCATE, KT_ACTIVATE, KT_EDGES, KT_COUNT };
 extern const char* const kKernelTypeNames[KT_COUNT];
 // Event log of one round: ev[0] before the first kernel, ev[i + 1] after
 // kernel i, whose type is type[i].
 struct Prof {
-  static constexpr int kMax = 4 + 2 * kPassesMax;
+  static constexpr int kMax = 5 + 2 * kPassesMax;
   cudaEvent_t ev[kMax + 1];
   int type[kMax];
   int n;
