@@ -81,6 +81,13 @@ vd_tree* vd_tree_new(int dim, const double* pts, int64_t n, int* status);
 /* Same, with all device work on the caller's CUDA stream (cudaStream_t). */
 vd_tree* vd_tree_new_on_stream(int dim, const double* pts, int64_t n, void* stream, int* status);
 void vd_tree_free(vd_tree* t);
+/* `new` from points already in device memory (n * dim doubles).  The super
+ * simplex is bit-identical to the host path's. */
+vd_tree* vd_tree_new_device(int dim, const double* d_pts, int64_t n, void* stream, int* status);
+/* Empties the tree and sizes its super simplex from new points (host /
+ * device), keeping every device allocation for reuse. */
+int vd_tree_reset(vd_tree* t, const double* pts, int64_t n);
+int vd_tree_reset_device(vd_tree* t, const double* d_pts, int64_t n);
 
 /* The super simplex `new` would build for `pts` (host computation only, no
  * device work): out[3*k + j] = coordinate j of super vertex k (z = 0 in 2D),
@@ -122,6 +129,8 @@ int vd_num_edges(vd_tree* t, int64_t* n);
 int vd_edges(vd_tree* t, int64_t* uv, int64_t cap, int64_t* n);
 /* Same into device memory as uint32 pairs. */
 int vd_edges_device(vd_tree* t, uint32_t* d_uv, int64_t cap, int64_t* n);
+/* Same into host memory as uint32 pairs (one copy). */
+int vd_edges_u32(vd_tree* t, uint32_t* uv, int64_t cap, int64_t* n);
 
 /* DelaunayTree::check_delaunay (src/delaunay_tree.rs:512-541, :642-671),
  * exact: *ok = 1 iff every simplex is positively oriented, adjacency is
@@ -158,12 +167,22 @@ int vd_set_tuning(vd_tree* t, int passes, int thin);
 int vd_profile(vd_tree* t, double* ms, int64_t* launches, int cap, int* n);
 const char* vd_profile_name(int i);
 int vd_set_trace(vd_tree* t, int on);
+/* Kernels launched by this library in this process so far. */
+int64_t vd_kernel_launches(void);
 int vd_trace(vd_tree* t, int64_t* rows, int64_t cap, int64_t* n);
 
 /* voronoids.delaunay(points) (src/lib.rs:104-125) in one call: new + insert
  * all points + sorted edge list.  `uv` may be NULL to query the count. */
 int vd_delaunay(int dim, const double* pts, int64_t n, uint64_t seed, int64_t* uv, int64_t cap,
                 int64_t* n_edges);
+/* The same on a reusable tree (its dimension is kept; allocations are
+ * reused): host points in, host uint32 edge pairs out (pinned buffers give
+ * full-speed copies). */
+int vd_delaunay_tree(vd_tree* t, const double* pts, int64_t n, uint64_t seed, uint32_t* uv, int64_t cap,
+                     int64_t* n_edges);
+/* The same with device points in and device uint32 edge pairs out. */
+int vd_delaunay_device(vd_tree* t, const double* d_pts, int64_t n, uint64_t seed, uint32_t* d_uv,
+                       int64_t cap, int64_t* n_edges);
 
 #ifdef __cplusplus
 }

@@ -20,11 +20,12 @@ VD_ERR_DUPLICATE = 4
 
 # Every symbol include/voronoids_gpu.h declares.
 EXPORTS = [
-    "vd_tree_new", "vd_tree_new_on_stream", "vd_tree_free", "vd_super_simplex", "vd_insert_points",
+    "vd_tree_new", "vd_tree_new_on_stream", "vd_tree_free", "vd_super_simplex", "vd_tree_new_device",
+    "vd_tree_reset", "vd_tree_reset_device", "vd_delaunay_tree", "vd_delaunay_device", "vd_edges_u32", "vd_insert_points",
     "vd_insert_points_device", "vd_insert_point", "vd_locate", "vd_num_vertices",
     "vd_max_simplex_id", "vd_num_simplices", "vd_simplices", "vd_num_edges", "vd_edges",
     "vd_edges_device", "vd_check_delaunay", "vd_duplicates", "vd_get_stats", "vd_status_str",
-    "vd_delaunay", "vd_set_schedule", "vd_set_tuning", "vd_set_profiling", "vd_profile", "vd_profile_name", "vd_set_trace", "vd_trace",
+    "vd_delaunay", "vd_set_schedule", "vd_set_tuning", "vd_set_profiling", "vd_profile", "vd_profile_name", "vd_set_trace", "vd_trace", "vd_kernel_launches",
 ]
 
 
@@ -58,6 +59,12 @@ def load(path=LIB_PATH):
         "vd_tree_new_on_stream": ([ctypes.c_int, dp, i64, vp, ip], vp),
         "vd_tree_free": ([vp], None),
         "vd_super_simplex": ([ctypes.c_int, dp, i64, dp, dp], ctypes.c_int),
+        "vd_tree_new_device": ([ctypes.c_int, vp, i64, vp, ip], vp),
+        "vd_tree_reset": ([vp, dp, i64], ctypes.c_int),
+        "vd_tree_reset_device": ([vp, vp, i64], ctypes.c_int),
+        "vd_delaunay_tree": ([vp, dp, i64, ctypes.c_uint64, vp, i64, i64p], ctypes.c_int),
+        "vd_delaunay_device": ([vp, vp, i64, ctypes.c_uint64, vp, i64, i64p], ctypes.c_int),
+        "vd_edges_u32": ([vp, vp, i64, i64p], ctypes.c_int),
         "vd_insert_points": ([vp, dp, i64, ctypes.c_uint64], ctypes.c_int),
         "vd_insert_points_device": ([vp, vp, i64, ctypes.c_uint64], ctypes.c_int),
         "vd_insert_point": ([vp, dp], ctypes.c_int),
@@ -81,6 +88,7 @@ def load(path=LIB_PATH):
         "vd_profile_name": ([ctypes.c_int], ctypes.c_char_p),
         "vd_set_trace": ([vp, ctypes.c_int], ctypes.c_int),
         "vd_trace": ([vp, i64p, i64, i64p], ctypes.c_int),
+        "vd_kernel_launches": ([], ctypes.c_int64),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -1140,6 +1140,7 @@ void round_impl(const DevTree& T, const Launch& L, int round, const Tuning& tu, 
     }
   };
   if (pf && pf->n == 0) cudaEventRecord(pf->ev[0], L.stream);
+  note_launches(4 + 2 * tu.passes - 1);
   k_pick<<<L.blocks, 256, 0, L.stream>>>(T, round);
   mark(KT_PICK);
   k_thin<D><<<L.blocks, 256, 0, L.stream>>>(T, round, tu.thin);
@@ -1162,6 +1163,7 @@ void round_impl(const DevTree& T, const Launch& L, int round, const Tuning& tu, 
 
 void launch_upload(const DevTree& T, const Launch& L, int dim, const double* d_xyz, int64_t n,
                    int base_vid, const int* super_order) {
+  note_launches(1);
   int4 sup = make_int4(super_order[0], super_order[1], super_order[2], super_order[3]);
   if (dim == 3)
     k_upload<3><<<L.blocks, 256, 0, L.stream>>>(T, d_xyz, n, base_vid, sup);
@@ -1171,6 +1173,7 @@ void launch_upload(const DevTree& T, const Launch& L, int dim, const double* d_x
 
 void launch_prefix_hist(const Launch& L, int64_t n, int base_vid, uint64_t seed,
                         const unsigned long long* thr, int nthr, int* d_counts) {
+  note_launches(1);
   Thresholds th;
   th.n = nthr;
   for (int k = 0; k < kMaxPrefixes; ++k) th.t[k] = k < nthr ? thr[k] : ~0ull;
@@ -1179,6 +1182,7 @@ void launch_prefix_hist(const Launch& L, int64_t n, int base_vid, uint64_t seed,
 
 void launch_activate(const DevTree& T, const Launch& L, int dim, int64_t n, int base_vid, uint64_t seed,
                      unsigned long long lo, unsigned long long hi, int round) {
+  note_launches(1);
   if (dim == 3)
     k_activate<3><<<L.blocks, 256, 0, L.stream>>>(T, n, base_vid, seed, lo, hi, round);
   else

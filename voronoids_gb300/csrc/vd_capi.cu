@@ -9,14 +9,18 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "../../include/voronoids_gpu.h"
 #include "vd_common.cuh"
 
 namespace vd {
+static std::atomic<long long> g_launches{0};
+void note_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+long long launches_total() { return g_launches.load(std::memory_order_relaxed); }
 int64_t run_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_in,
-                  const EdgeScratch& S, uint2* d_out, int* d_total_pair, int* h_total_pair);
+                  const EdgeScratch& S, uint2* d_out, int64_t cap_out, int* d_total_pair, int* h_total_pair);
 }
 
 namespace {
@@ -60,9 +64,8 @@ void ref_bounding_sphere(int dim, const double* pts, int64_t n, double* center, 
   *radius = r;
 }
 
-void ref_super_vertices(int dim, const double* pts, int64_t n, double out[4][3], double* R) {
-  double c[3] = {0, 0, 0}, r;
-  ref_bounding_sphere(dim, pts, n, c, &r);
+// Super vertices for bounding centre c and radius r (src/delaunay_tree.rs:392-406, :547-558).
+void ref_super_from_sphere(int dim, const double* c, double r, double out[4][3], double* R) {
   r *= 10.0;
   *R = r;
   const double pi = 3.141592653589793;
@@ -80,6 +83,12 @@ void ref_super_vertices(int dim, const double* pts, int64_t n, double out[4][3],
     memcpy(out, v, sizeof(v));
     out[3][0] = out[3][1] = out[3][2] = 0.0;
   }
+}
+
+void ref_super_vertices(int dim, const double* pts, int64_t n, double out[4][3], double* R) {
+  double c[3] = {0, 0, 0}, r;
+  ref_bounding_sphere(dim, pts, n, c, &r);
+  ref_super_from_sphere(dim, c, r, out, R);
 }
 
 bool coord_ok(double a) {
@@ -116,6 +125,7 @@ struct vd_tree {
   int64_t cap_verts = 0;
   int64_t cap_act = 0;
   int round = 0;
+  int round_base = 0;  // first round of the current triangulation
   int64_t inserted = 0;   // vertices inserted (from counters)
   int64_t calls = 0;
   DevTree T = {};
@@ -133,6 +143,15 @@ struct vd_tree {
   int* d_misc = nullptr;      // small device scratch (live-slot search, locate)
   int64_t* d_loc = nullptr;
   int64_t cap_loc = 0;
+  int64_t ncells = 0;
+  // pinned staging for small host<->device copies
+  vdp::VPt h_sv[4];
+  vdp::FPt h_sf[4];
+  vd::Simplex h_s0;
+  unsigned long long* h_mm = nullptr;
+  // device staging of host input points (one-shot host path)
+  double* d_in = nullptr;
+  int64_t cap_in = 0;
   // insertion schedule (priority prefixes)
   int64_t first_prefix = 64;
   double growth = 4.0;
@@ -335,6 +354,9 @@ void release(vd_tree* t) {
   dfree(t->T.wchunk);
   if (t->h_counts) cudaFreeHost(t->h_counts);
   t->h_counts = nullptr;
+  if (t->h_mm) cudaFreeHost(t->h_mm);
+  t->h_mm = nullptr;
+  dfree(t->d_in);
   if (t->hctr) cudaFreeHost(t->hctr);
   if (t->h_pair) cudaFreeHost(t->h_pair);
   t->hctr = nullptr;
@@ -346,38 +368,11 @@ void release(vd_tree* t) {
   t->stream = nullptr;
 }
 
-int init_tree(vd_tree* t, int dim, const double* pts, int64_t n, void* stream) {
-  if ((dim != 2 && dim != 3) || n < 1 || !pts) return vd::E_ARG;
-  for (int64_t i = 0; i < n * dim; ++i) {
-    if (!isfinite(pts[i])) return vd::E_NONFINITE;
-    if (!coord_ok(pts[i])) return vd::E_RANGE;
-  }
+// Device, stream and pools of an empty tree of dimension `dim`.
+int alloc_tree(vd_tree* t, int dim, void* stream) {
   t->dim = dim;
   t->ns = dim + 1;
   t->tuning = dim == 3 ? vd::Tuning{2, 2} : vd::Tuning{3, 1};
-  ref_super_vertices(dim, pts, n, t->sup, &t->R);
-  if (!(t->R > 0.0) || !isfinite(t->R)) return vd::E_DEGENERATE;
-  for (int i = 0; i < t->ns; ++i)
-    for (int j = 0; j < 3; ++j)
-      if (!isfinite(t->sup[i][j]) || !coord_ok(t->sup[i][j])) return vd::E_RANGE;
-  // positive orientation of the super simplex
-  {
-    vdp::VPt v[4];
-    for (int i = 0; i < 4; ++i) v[i] = vdp::VPt{t->sup[i][0], t->sup[i][1], t->sup[i][2], 0.0};
-    vdp::Tally tl = {0, 0, 0, 0};
-    int err = 0;
-    int neg = dim == 3 ? vdp::exit_face<3, true>(v, v[3], 1u << 3, tl, err)
-                       : vdp::exit_face<2, true>(v, v[2], 1u << 2, tl, err);
-    if (neg >= 0) {
-      // orientation <= 0: swap the first two (zero would be degenerate)
-      std::swap(t->sup_order[0], t->sup_order[1]);
-      vdp::VPt w[4] = {v[1], v[0], v[2], v[3]};
-      int neg2 = dim == 3 ? vdp::exit_face<3, true>(w, w[3], 1u << 3, tl, err)
-                          : vdp::exit_face<2, true>(w, w[2], 1u << 2, tl, err);
-      if (neg2 >= 0) return vd::E_DEGENERATE;
-    }
-    if (dim == 2) t->sup_order[3] = -1;
-  }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return vd::E_CUDA;
   t->device = dev;
@@ -392,56 +387,138 @@ int init_tree(vd_tree* t, int dim, const double* pts, int64_t n, void* stream) {
     t->own_stream = true;
   }
   if (cudaMallocHost((void**)&t->hctr, sizeof(Counters)) != cudaSuccess) return vd::E_NOMEM;
-  if (cudaMallocHost((void**)&t->h_pair, 4 * sizeof(int)) != cudaSuccess) return vd::E_NOMEM;
+  if (cudaMallocHost((void**)&t->h_pair, 16 * sizeof(int)) != cudaSuccess) return vd::E_NOMEM;
   memset(t->hctr, 0, sizeof(Counters));
   if (dalloc(&t->T.ctr, 1) || dalloc(&t->d_pair, 4) || dalloc(&t->d_check, 8) ||
       dalloc(&t->d_misc, 16) || dalloc(&t->d_counts, vd::kMaxPrefixes))
     return vd::E_NOMEM;
   if (cudaMallocHost((void**)&t->h_counts, sizeof(int) * vd::kMaxPrefixes) != cudaSuccess) return vd::E_NOMEM;
+  if (cudaMallocHost((void**)&t->h_mm, 8 * sizeof(unsigned long long)) != cudaSuccess) return vd::E_NOMEM;
   t->T.cap_wchunk = t->sms * 20;
   if (dalloc(&t->T.wchunk, t->T.cap_wchunk)) return vd::E_NOMEM;
-  cudaMemsetAsync(t->T.wchunk, 0, sizeof(int2) * t->T.cap_wchunk, t->stream);
-  // hint grid over the sizing box (centre +- bounding radius)
   t->T.hint_levels = dim == 3 ? 6 : 9;
-  const int64_t ncells = dim == 3 ? ((1LL << (3 * (t->T.hint_levels + 1))) - 1) / 7
-                                  : ((1LL << (2 * (t->T.hint_levels + 1))) - 1) / 3;
-  if (dalloc(&t->T.hint, ncells)) return vd::E_NOMEM;
-  cudaMemsetAsync(t->T.hint, 0xff, sizeof(int) * ncells, t->stream);
-  {
-    double c[3] = {0, 0, 0}, rb = 0;
-    ref_bounding_sphere(dim, pts, n, c, &rb);
-    for (int k = 0; k < 3; ++k) t->T.gorg[k] = (k < dim ? c[k] : 0.0) - rb;
-    t->T.gscale = rb > 0 ? 1.0 / (2.0 * rb) : 1.0;
-  }
-  cudaMemsetAsync(t->T.ctr, 0, sizeof(Counters), t->stream);
-  // vertices: super first
-  t->cap_verts = t->ns + std::max<int64_t>(n, 16);
+  t->ncells = dim == 3 ? ((1LL << (3 * (t->T.hint_levels + 1))) - 1) / 7
+                       : ((1LL << (2 * (t->T.hint_levels + 1))) - 1) / 3;
+  if (dalloc(&t->T.hint, t->ncells)) return vd::E_NOMEM;
+  t->cap_verts = t->ns + 16;
   if (dalloc(&t->T.pts, t->cap_verts) || dalloc(&t->T.ptf, t->cap_verts)) return vd::E_NOMEM;
   t->T.cap_verts = (int)t->cap_verts;
-  std::vector<vdp::VPt> sv(t->ns);
-  for (int i = 0; i < t->ns; ++i) sv[i] = vdp::VPt{t->sup[i][0], t->sup[i][1], t->sup[i][2], 0.0};
-  cudaMemcpyAsync(t->T.pts, sv.data(), sizeof(vdp::VPt) * t->ns, cudaMemcpyHostToDevice, t->stream);
-  std::vector<vdp::FPt> sf(t->ns);
-  for (int i = 0; i < t->ns; ++i) sf[i] = vdp::split_point(t->sup[i][0], t->sup[i][1], t->sup[i][2]);
-  cudaMemcpyAsync(t->T.ptf, sf.data(), sizeof(vdp::FPt) * t->ns, cudaMemcpyHostToDevice, t->stream);
-  t->nverts = t->ns;
-  // simplex pool with the super simplex in slot 0
   t->T.cap_simp = 0;
   t->hctr->nsimp = 0;
-  t->hctr->nsimp = 0;
   if (ensure_simplices(t, 1024)) return vd::E_NOMEM;
-  vd::Simplex s0;
-  for (int i = 0; i < 4; ++i) {
-    s0.v[i] = t->sup_order[i];
-    s0.n[i] = -1;
+  return vd::E_OK;
+}
+
+// (Re)starts the tree as the single super simplex for the bounding sphere
+// (centre c, radius rb) of the sizing points.  Pools keep their capacity.
+int set_geometry(vd_tree* t, const double* c, double rb) {
+  const int dim = t->dim;
+  ref_super_from_sphere(dim, c, rb, t->sup, &t->R);
+  if (!(t->R > 0.0) || !isfinite(t->R)) return vd::E_DEGENERATE;
+  for (int i = 0; i < t->ns; ++i)
+    for (int j = 0; j < 3; ++j)
+      if (!isfinite(t->sup[i][j]) || !coord_ok(t->sup[i][j])) return vd::E_RANGE;
+  t->sup_order[0] = 0;
+  t->sup_order[1] = 1;
+  t->sup_order[2] = 2;
+  t->sup_order[3] = dim == 3 ? 3 : -1;
+  {  // positive orientation of the super simplex
+    vdp::VPt v[4];
+    for (int i = 0; i < 4; ++i) v[i] = vdp::VPt{t->sup[i][0], t->sup[i][1], t->sup[i][2], 0.0};
+    vdp::Tally tl = {0, 0, 0, 0};
+    int err = 0;
+    int neg = dim == 3 ? vdp::exit_face<3, true>(v, v[3], 1u << 3, tl, err)
+                       : vdp::exit_face<2, true>(v, v[2], 1u << 2, tl, err);
+    if (neg >= 0) {
+      std::swap(t->sup_order[0], t->sup_order[1]);
+      vdp::VPt w[4] = {v[1], v[0], v[2], v[3]};
+      int neg2 = dim == 3 ? vdp::exit_face<3, true>(w, w[3], 1u << 3, tl, err)
+                          : vdp::exit_face<2, true>(w, w[2], 1u << 2, tl, err);
+      if (neg2 >= 0) return vd::E_DEGENERATE;
+    }
   }
-  cudaMemcpyAsync(t->T.simp, &s0, sizeof(s0), cudaMemcpyHostToDevice, t->stream);
-  Counters init;
-  memset(&init, 0, sizeof(init));
-  init.nsimp = 1;
-  *t->hctr = init;
-  cudaMemcpyAsync(t->T.ctr, &init, sizeof(init), cudaMemcpyHostToDevice, t->stream);
+  for (int k = 0; k < 3; ++k) t->T.gorg[k] = (k < dim ? c[k] : 0.0) - rb;
+  t->T.gscale = rb > 0 ? 1.0 / (2.0 * rb) : 1.0;
+  cudaMemsetAsync(t->T.hint, 0xff, sizeof(int) * t->ncells, t->stream);
+  cudaMemsetAsync(t->T.wchunk, 0, sizeof(int2) * t->T.cap_wchunk, t->stream);
+  for (int i = 0; i < t->ns; ++i) {
+    t->h_sv[i] = vdp::VPt{t->sup[i][0], t->sup[i][1], t->sup[i][2], 0.0};
+    t->h_sf[i] = vdp::split_point(t->sup[i][0], t->sup[i][1], t->sup[i][2]);
+  }
+  cudaMemcpyAsync(t->T.pts, t->h_sv, sizeof(vdp::VPt) * t->ns, cudaMemcpyHostToDevice, t->stream);
+  cudaMemcpyAsync(t->T.ptf, t->h_sf, sizeof(vdp::FPt) * t->ns, cudaMemcpyHostToDevice, t->stream);
+  t->nverts = t->ns;
+  t->inserted = 0;
+  t->round_base = t->round;
+  t->edges_valid = false;
+  for (int i = 0; i < 4; ++i) {
+    t->h_s0.v[i] = t->sup_order[i];
+    t->h_s0.n[i] = -1;
+  }
+  cudaMemcpyAsync(t->T.simp, &t->h_s0, sizeof(vd::Simplex), cudaMemcpyHostToDevice, t->stream);
+  memset(t->hctr, 0, sizeof(Counters));
+  t->hctr->nsimp = 1;
+  cudaMemcpyAsync(t->T.ctr, t->hctr, sizeof(Counters), cudaMemcpyHostToDevice, t->stream);
   return cuda_status(cudaStreamSynchronize(t->stream));
+}
+
+int check_host_points(int dim, const double* pts, int64_t n) {
+  if ((dim != 2 && dim != 3) || n < 1 || !pts) return vd::E_ARG;
+  for (int64_t i = 0; i < n * dim; ++i) {
+    if (!isfinite(pts[i])) return vd::E_NONFINITE;
+    if (!coord_ok(pts[i])) return vd::E_RANGE;
+  }
+  return vd::E_OK;
+}
+
+int init_tree(vd_tree* t, int dim, const double* pts, int64_t n, void* stream) {
+  int rc = check_host_points(dim, pts, n);
+  if (rc) return rc;
+  double c[3] = {0, 0, 0}, rb = 0;
+  ref_bounding_sphere(dim, pts, n, c, &rb);
+  rc = alloc_tree(t, dim, stream);
+  if (rc) return rc;
+  return set_geometry(t, c, rb);
+}
+
+// Bounding sphere of n device points (same result as the reference's loop).
+int size_from_device(vd_tree* t, const double* d_pts, int64_t n, double* c, double* rb) {
+  if (n < 1 || !d_pts) return vd::E_ARG;
+  const int dim = t->dim;
+  const vd::Launch L = launch_of(t);
+  unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0, 0, 0};
+  memcpy(t->h_mm, init, sizeof(init));
+  unsigned long long* d_mm = reinterpret_cast<unsigned long long*>(t->d_misc);
+  cudaMemcpyAsync(d_mm, t->h_mm, sizeof(init), cudaMemcpyHostToDevice, t->stream);
+  vd::launch_bbox(L, dim, d_pts, n, d_mm);
+  cudaMemcpyAsync(t->h_mm, d_mm, sizeof(init), cudaMemcpyDeviceToHost, t->stream);
+  if (cudaStreamSynchronize(t->stream) != cudaSuccess) return vd::E_CUDA;
+  double lo[3], hi[3];
+  for (int k = 0; k < dim; ++k) {
+    auto dec = [](unsigned long long key) {
+      const unsigned long long b = (key >> 63) ? (key & 0x7fffffffffffffffull) : ~key;
+      double x;
+      memcpy(&x, &b, 8);
+      return x;
+    };
+    lo[k] = dec(t->h_mm[k]);
+    hi[k] = dec(t->h_mm[3 + k]);
+    if (!isfinite(lo[k]) || !isfinite(hi[k])) return vd::E_NONFINITE;
+    c[k] = (hi[k] + lo[k]) / 2.0;
+  }
+  for (int k = dim; k < 3; ++k) c[k] = 0.0;
+  double su = 0.0, sl = 0.0;
+  for (int i = 0; i < dim; ++i) su += (hi[i] - c[i]) * (hi[i] - c[i]);
+  for (int i = 0; i < dim; ++i) sl += (lo[i] - c[i]) * (lo[i] - c[i]);
+  const double ud = sqrt(su), ld = sqrt(sl);
+  const double r0 = ud > ld ? ud : ld;
+  int* d_flag = t->d_misc + 12;
+  cudaMemsetAsync(d_flag, 0, sizeof(int), t->stream);
+  vd::launch_outside(L, dim, d_pts, n, c, r0, d_flag);
+  cudaMemcpyAsync(t->h_pair + 8, d_flag, sizeof(int), cudaMemcpyDeviceToHost, t->stream);
+  if (cudaStreamSynchronize(t->stream) != cudaSuccess) return vd::E_CUDA;
+  *rb = t->h_pair[8] ? r0 * 1.5 : r0;
+  return vd::E_OK;
 }
 
 vd::Launch sized_launch(const vd_tree* t, int64_t items) {
@@ -579,6 +656,7 @@ int insert_device(vd_tree* t, const double* d_xyz, int64_t n, uint64_t seed) {
     carried = t->hctr->nact[r & 1];
   }
   t->round = r;
+  vd::launch_close_chunks(t->T, L);
   if (!rc) rc = sync_counters(t);
   t->inserted = t->hctr->ninserted;
   if (rc) return rc;
@@ -628,8 +706,13 @@ int ensure_edge_scratch(vd_tree* t, int64_t n_in, int64_t nsimp) {
   return vd::E_OK;
 }
 
-int compute_edges(vd_tree* t) {
-  if (t->edges_valid) return vd::E_OK;
+// Edge list into `out` (device, capacity `cap`), or into the tree's own
+// buffer when out is null.  *m receives the count (which may exceed cap).
+int compute_edges(vd_tree* t, uint2* out = nullptr, int64_t cap = 0, int64_t* m = nullptr) {
+  if (t->edges_valid && !out) {
+    if (m) *m = t->nedges;
+    return vd::E_OK;
+  }
   int rc = sync_counters(t);
   if (rc) return rc;
   const int64_t n_in = t->nverts - t->ns;
@@ -637,15 +720,18 @@ int compute_edges(vd_tree* t) {
   if ((t->dim == 3 ? 6 : 3) * nsimp > 0x7fffff00LL) return vd::E_NOMEM;
   rc = ensure_edge_scratch(t, n_in, nsimp);
   if (rc) return rc;
-  int64_t m;
+  int64_t got;
   {
     ScopedProf sp(t, vd::KT_EDGES);
-    m = vd::run_edges(t->T, launch_of(t), t->dim, (int)nsimp, (int)n_in, t->es, t->d_edges, t->d_pair,
-                      t->h_pair);
+    got = vd::run_edges(t->T, launch_of(t), t->dim, (int)nsimp, (int)n_in, t->es, out ? out : t->d_edges,
+                        out ? cap : t->cap_edges, t->d_pair, t->h_pair);
   }
-  if (m < 0) return vd::E_CUDA;
-  t->nedges = m;
-  t->edges_valid = true;
+  if (got < 0) return vd::E_CUDA;
+  if (m) *m = got;
+  if (!out) {
+    t->nedges = got;
+    t->edges_valid = true;
+  }
   return vd::E_OK;
 }
 
@@ -698,6 +784,67 @@ int vd_super_simplex(int dim, const double* pts, int64_t n, double* out, double*
   for (int k = 0; k <= dim; ++k)
     for (int j = 0; j < 3; ++j) out[3 * k + j] = sv[k][j];
   return VD_OK;
+}
+
+vd_tree* vd_tree_new_device(int dim, const double* d_pts, int64_t n, void* stream, int* status) {
+  vd_tree* t = new (std::nothrow) vd_tree();
+  if (!t) {
+    if (status) *status = VD_ERR_NOMEM;
+    return nullptr;
+  }
+  int rc = (dim == 2 || dim == 3) && n >= 1 && d_pts ? alloc_tree(t, dim, stream) : VD_ERR_ARG;
+  double c[3], rb;
+  if (!rc) rc = size_from_device(t, d_pts, n, c, &rb);
+  if (!rc) rc = set_geometry(t, c, rb);
+  if (status) *status = rc;
+  return t;
+}
+
+int vd_tree_reset(vd_tree* t, const double* pts, int64_t n) {
+  if (!t || !t->hctr) return VD_ERR_ARG;
+  int rc = check_host_points(t->dim, pts, n);
+  if (rc) return rc;
+  double c[3] = {0, 0, 0}, rb = 0;
+  ref_bounding_sphere(t->dim, pts, n, c, &rb);
+  return set_geometry(t, c, rb);
+}
+
+int vd_tree_reset_device(vd_tree* t, const double* d_pts, int64_t n) {
+  if (!t || !t->hctr) return VD_ERR_ARG;
+  double c[3], rb;
+  int rc = size_from_device(t, d_pts, n, c, &rb);
+  if (rc) return rc;
+  return set_geometry(t, c, rb);
+}
+
+int vd_delaunay_device(vd_tree* t, const double* d_pts, int64_t n, uint64_t seed, uint32_t* d_uv, int64_t cap,
+                       int64_t* n_edges) {
+  if (!t || !t->hctr || (t->dim != 2 && t->dim != 3)) return VD_ERR_ARG;
+  int rc = vd_tree_reset_device(t, d_pts, n);
+  if (rc) return rc;
+  rc = insert_device(t, d_pts, n, seed);
+  if (rc == VD_OK && t->hctr->ndup > 0) rc = VD_ERR_DUPLICATE;
+  if (rc && rc != VD_ERR_DUPLICATE) return rc;
+  const int rc2 = vd_edges_device(t, d_uv, cap, n_edges);
+  return rc2 ? rc2 : rc;
+}
+
+int vd_delaunay_tree(vd_tree* t, const double* pts, int64_t n, uint64_t seed, uint32_t* uv, int64_t cap,
+                     int64_t* n_edges) {
+  if (!t || !t->hctr || !pts || n < 1) return VD_ERR_ARG;
+  if (n * t->dim > t->cap_in) {
+    dfree(t->d_in);
+    if (dalloc(&t->d_in, (size_t)(n * t->dim))) return VD_ERR_NOMEM;
+    t->cap_in = n * t->dim;
+  }
+  cudaMemcpyAsync(t->d_in, pts, sizeof(double) * n * t->dim, cudaMemcpyHostToDevice, t->stream);
+  int rc = vd_tree_reset_device(t, t->d_in, n);
+  if (rc) return rc;
+  rc = insert_device(t, t->d_in, n, seed);
+  if (rc == VD_OK && t->hctr->ndup > 0) rc = VD_ERR_DUPLICATE;
+  if (rc && rc != VD_ERR_DUPLICATE) return rc;
+  const int rc2 = vd_edges_u32(t, uv, cap, n_edges);
+  return rc2 ? rc2 : rc;
 }
 
 void vd_tree_free(vd_tree* t) {
@@ -778,7 +925,7 @@ int vd_simplices(vd_tree* t, int32_t* verts, int32_t* nbrs, int64_t cap, int64_t
 
 int vd_num_edges(vd_tree* t, int64_t* n) {
   if (ready(t) || !n) return VD_ERR_ARG;
-  int rc = compute_edges(t);
+  int rc = compute_edges(t, nullptr, 0, nullptr);
   if (rc) return rc;
   *n = t->nedges;
   return VD_OK;
@@ -786,7 +933,7 @@ int vd_num_edges(vd_tree* t, int64_t* n) {
 
 int vd_edges(vd_tree* t, int64_t* uv, int64_t cap, int64_t* n) {
   if (ready(t)) return VD_ERR_ARG;
-  int rc = compute_edges(t);
+  int rc = compute_edges(t, nullptr, 0, nullptr);
   if (rc) return rc;
   if (n) *n = t->nedges;
   if (!uv) return VD_OK;
@@ -803,12 +950,21 @@ int vd_edges(vd_tree* t, int64_t* uv, int64_t cap, int64_t* n) {
 
 int vd_edges_device(vd_tree* t, uint32_t* d_uv, int64_t cap, int64_t* n) {
   if (ready(t)) return VD_ERR_ARG;
-  int rc = compute_edges(t);
+  int64_t m = 0;
+  int rc = d_uv ? compute_edges(t, reinterpret_cast<uint2*>(d_uv), cap, &m) : compute_edges(t, nullptr, 0, &m);
+  if (rc) return rc;
+  if (n) *n = m;
+  return (d_uv && m > cap) ? VD_ERR_ARG : VD_OK;
+}
+
+int vd_edges_u32(vd_tree* t, uint32_t* uv, int64_t cap, int64_t* n) {
+  if (ready(t)) return VD_ERR_ARG;
+  int rc = compute_edges(t, nullptr, 0, nullptr);
   if (rc) return rc;
   if (n) *n = t->nedges;
-  if (!d_uv) return VD_OK;
+  if (!uv) return VD_OK;
   if (cap < t->nedges) return VD_ERR_ARG;
-  cudaMemcpyAsync(d_uv, t->d_edges, sizeof(uint2) * t->nedges, cudaMemcpyDeviceToDevice, t->stream);
+  cudaMemcpyAsync(uv, t->d_edges, sizeof(uint2) * t->nedges, cudaMemcpyDeviceToHost, t->stream);
   return cuda_status(cudaStreamSynchronize(t->stream));
 }
 
@@ -853,7 +1009,7 @@ int vd_get_stats(vd_tree* t, vd_stats* s) {
   int rc = sync_counters(t);
   if (rc) return rc;
   const Counters& h = *t->hctr;
-  s->rounds = t->round;
+  s->rounds = t->round - t->round_base;
   s->inserted = h.ninserted;
   s->duplicates = h.ndup;
   s->live_simplices = 1 + (int64_t)h.created - (int64_t)h.killed;
@@ -918,6 +1074,8 @@ int vd_profile(vd_tree* t, double* ms, int64_t* launches, int cap, int* n) {
   }
   return VD_OK;
 }
+
+int64_t vd_kernel_launches(void) { return (int64_t)vd::launches_total(); }
 
 const char* vd_profile_name(int i) {
   if (i >= 0 && i < vd::KT_COUNT) return vd::kKernelTypeNames[i];

@@ -79,6 +79,7 @@ __global__ void k_check(DevTree T, int nsimp, unsigned long long* out) {
 }  // namespace
 
 void launch_check(const DevTree& T, const Launch& L, int dim, int nsimp, unsigned long long* d_out) {
+  note_launches(1);
   cudaMemsetAsync(d_out, 0, 6 * sizeof(unsigned long long), L.stream);
   if (dim == 3)
     k_check<3><<<L.blocks, 256, 0, L.stream>>>(T, nsimp, d_out);

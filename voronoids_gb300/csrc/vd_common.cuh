@@ -155,6 +155,10 @@ __device__ inline bool bad_simp(const DevTree& T, int s) { return (unsigned)s >=
 __device__ inline bool bad_vert(const DevTree& T, int v) { return (unsigned)v >= (unsigned)T.cap_verts; }
 #endif
 
+// Kernels launched by this library in this process (diagnostics).
+void note_launches(long long k);
+long long launches_total();
+
 // Host-side launchers (vd_build.cu, vd_edges.cu, vd_check.cu).
 struct Launch {
   int blocks;      // persistent grid size for thread-per-item kernels
@@ -202,6 +206,12 @@ struct EdgeScratch {
 int64_t scan_scratch_ints(int64_t n);
 void launch_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_in,
                   const EdgeScratch& S, uint2* d_out);
+
+// Device sizing of the super simplex (vd_size.cu).
+void launch_bbox(const Launch& L, int dim, const double* d_xyz, int64_t n, unsigned long long* d_mm);
+void launch_outside(const Launch& L, int dim, const double* d_xyz, int64_t n, const double* c, double r0,
+                    int* d_flag);
+void launch_close_chunks(const DevTree& T, const Launch& L);
 
 // Validator: out[0..5] = non-positive, asymmetric, not Delaunay (exact),
 // not perturbed-Delaunay, hull facets, facets checked.

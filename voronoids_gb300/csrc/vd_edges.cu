@@ -80,6 +80,7 @@ void exclusive_scan(const int* in, int* out, long long n, int* tmp, cudaStream_t
   const long long tiles = (n + kScanTile - 1) / kScanTile;
   int* sums = tmp;
   k_scan_tile<<<(unsigned)tiles, kScanBlock, 0, st>>>(in, out, sums, n);
+  note_launches(1);
   if (tiles == 1) {
     cudaMemcpyAsync(out + n, sums, sizeof(int), cudaMemcpyDeviceToDevice, st);
     return;
@@ -87,6 +88,7 @@ void exclusive_scan(const int* in, int* out, long long n, int* tmp, cudaStream_t
   int* scanned = tmp + tiles;
   exclusive_scan(sums, scanned, tiles, scanned + tiles + 1, st);
   k_scan_add<<<(unsigned)tiles, 256, 0, st>>>(out, scanned, n);
+  note_launches(1);
   cudaMemcpyAsync(out + n, scanned + tiles, sizeof(int), cudaMemcpyDeviceToDevice, st);
 }
 
@@ -229,12 +231,13 @@ __global__ void __launch_bounds__(1024) k_edge_uniq_big(const int* big, const in
 }
 
 __global__ void k_edge_out(int n_in, const int* off, const int* buf, const int* ucnt,
-                           const int* uoff, uint2* out) {
+                           const int* uoff, uint2* out, long long cap) {
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int u = w; u < n_in; u += nw) {
     const int b = off[u], o = uoff[u], c = ucnt[u];
-    for (int k = lane; k < c; k += 32) out[o + k] = make_uint2((unsigned)u, (unsigned)buf[b + k]);
+    for (int k = lane; k < c; k += 32)
+      if (o + k < cap) out[o + k] = make_uint2((unsigned)u, (unsigned)buf[b + k]);
   }
 }
 
@@ -252,8 +255,9 @@ int64_t scan_scratch_ints(int64_t n) {
 
 // Returns the number of unique edges written to d_out (or -1 on a CUDA error).
 int64_t run_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_in,
-                  const EdgeScratch& S, uint2* d_out, int* d_total_pair, int* h_total_pair) {
+                  const EdgeScratch& S, uint2* d_out, int64_t cap_out, int* d_total_pair, int* h_total_pair) {
   cudaStream_t st = L.stream;
+  note_launches(4);  // count, fill, unique, output (scans count themselves)
   cudaMemsetAsync(S.cnt, 0, sizeof(int) * (n_in + 1), st);
   cudaMemsetAsync(S.nbig, 0, sizeof(int), st);
   if (dim == 3) {
@@ -269,7 +273,7 @@ int64_t run_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_i
   }
   k_edge_uniq<<<L.blocks, 256, 0, st>>>(n_in, S.off, S.buf, S.ucnt, S.big, S.nbig);
   exclusive_scan(S.ucnt, S.uoff, n_in, S.scan_tmp, st);
-  k_edge_out<<<L.blocks, 256, 0, st>>>(n_in, S.off, S.buf, S.ucnt, S.uoff, d_out);
+  k_edge_out<<<L.blocks, 256, 0, st>>>(n_in, S.off, S.buf, S.ucnt, S.uoff, d_out, cap_out);
   cudaMemcpyAsync(d_total_pair, S.uoff + n_in, sizeof(int), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(d_total_pair + 1, S.nbig, sizeof(int), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(h_total_pair, d_total_pair, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -298,8 +302,9 @@ int64_t run_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_i
   }
   cudaMemcpyAsync(dsoff, soff.data(), sizeof(long long) * (nbig + 1), cudaMemcpyHostToDevice, st);
   k_edge_uniq_big<<<nbig, 1024, 0, st>>>(S.big, S.off, S.buf, S.ucnt, scratch, dsoff);
+  note_launches(2);
   exclusive_scan(S.ucnt, S.uoff, n_in, S.scan_tmp, st);
-  k_edge_out<<<L.blocks, 256, 0, st>>>(n_in, S.off, S.buf, S.ucnt, S.uoff, d_out);
+  k_edge_out<<<L.blocks, 256, 0, st>>>(n_in, S.off, S.buf, S.ucnt, S.uoff, d_out, cap_out);
   cudaMemcpyAsync(h_total_pair, S.uoff + n_in, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaError_t e = cudaStreamSynchronize(st);
   cudaFree(scratch);
