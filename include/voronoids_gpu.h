@@ -184,6 +184,27 @@ int vd_delaunay_tree(vd_tree* t, const double* pts, int64_t n, uint64_t seed, ui
 int vd_delaunay_device(vd_tree* t, const double* d_pts, int64_t n, uint64_t seed, uint32_t* d_uv,
                        int64_t cap, int64_t* n_edges);
 
+/* Sorted edge list of a caller-owned simplex list, for callers that may not
+ * allocate GPU memory (for example an application whose memory manager owns
+ * the whole device, or a loop that cannot afford the synchronisation of a
+ * cudaMalloc).  No counterpart in the reference.  It allocates nothing: its
+ * scratch is one statically sized device array (about 10.5 MB) that every GPU
+ * loading this library holds until the process exits.
+ *   d_simp  device array of ns rows of 4 int32 vertex ids (16-byte aligned);
+ *           negative ids (super vertices, the unused 4th id in 2D) are skipped
+ *   ns <= 131072 simplices, vertex ids < nverts <= 65536; larger inputs are
+ *           rejected with VD_ERR_ARG
+ *   d_uv    device output, (u, v) uint32 pairs, u < v, sorted; *n_edges gets
+ *           the count (VD_ERR_ARG if it exceeds cap)
+ *   stream  cudaStream_t (NULL = default stream); the call returns after its
+ *           work on that stream has finished.
+ * All calls on a device share the scratch array and leave their data in it;
+ * calls whose GPU work overlaps race and give wrong results.  The first call
+ * on a device looks up the array's address (cudaGetSymbolAddress) with that
+ * device current; make it before starting any stream capture. */
+int vd_edges_from_simplices_noalloc(int dim, const int32_t* d_simp, int64_t ns, int64_t nverts,
+                                    uint32_t* d_uv, int64_t cap, int64_t* n_edges, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
