@@ -153,7 +153,8 @@ const char* vd_status_str(int status);
  * resets the sums.  The trace synchronises after every round and keeps one
  * row per round: round, active points at start, cumulative nominations,
  * cumulative searches, cumulative insertions, cumulative conflict tests,
- * cumulative walk steps, active points after the round. */
+ * GPU microseconds of the round (-1 unless profiling is on), active points
+ * after the round. */
 int vd_set_profiling(vd_tree* t, int on);
 /* Insertion schedule (no reference counterpart: the reference inserts all of
  * a batch against one queue, src/scheduler.rs:6-55): points are inserted in

@@ -544,13 +544,20 @@ int run_rounds(vd_tree* t, const vd::Launch& L, int& r, int64_t stop) {
     accumulate_events(t, chunk);
     Counters& h = *t->hctr;
     if (t->trace) {
+      // GPU time of the round in microseconds when profiling is on
+      int64_t us = -1;
+      if (t->prof && !t->profs.empty() && t->profs[0].n > 0) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, t->profs[0].ev[0], t->profs[0].ev[t->profs[0].n]) == cudaSuccess)
+          us = (int64_t)(ms * 1000.0f);
+      }
       const int64_t row[8] = {r - 1,
                               (int64_t)h.nact[(r - 1) & 1],
                               (int64_t)h.candidates,
                               (int64_t)h.searched,
                               (int64_t)h.ninserted,
                               (int64_t)h.cavity_tests,
-                              (int64_t)h.walk,
+                              us,
                               (int64_t)h.nact[r & 1]};
       t->trace_rows.insert(t->trace_rows.end(), row, row + 8);
     }
