@@ -156,11 +156,13 @@ const char* vd_status_str(int status);
  * GPU microseconds of the round (-1 unless profiling is on), active points
  * after the round. */
 int vd_set_profiling(vd_tree* t, int on);
-/* Insertion schedule (no reference counterpart: the reference inserts all of
- * a batch against one queue, src/scheduler.rs:6-55): points are inserted in
- * priority prefixes of `first_prefix` points, then growing by `growth` (>= 1.5)
- * per prefix.  Defaults 64 and 4. */
-int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth);
+/* Insertion schedule (no reference counterpart: the reference places all
+ * points of a batch in rounds up front, src/scheduler.rs:6-55).  The points
+ * of a call are split by priority into levels of `first_prefix` points, then
+ * growing by `growth` (1 < growth <= 16); a round activates further levels
+ * while fewer than `ratio` (0 < ratio <= 64) times the inserted points are
+ * active.  Defaults 64, 1.25 and 0.4. */
+int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth, double ratio);
 /* Round tuning: resolution passes per round (1..6) and the thinning radius
  * (1 = a nominee must hold its simplex and face neighbours, 2 = and no lower
  * nominee two faces away).  Defaults: 3D 2 passes / radius 2, 2D 3 / 1. */

@@ -82,7 +82,7 @@ def load(path=LIB_PATH):
         "vd_status_str": ([ctypes.c_int], ctypes.c_char_p),
         "vd_delaunay": ([ctypes.c_int, dp, i64, ctypes.c_uint64, i64p, i64, i64p], ctypes.c_int),
         "vd_set_profiling": ([vp, ctypes.c_int], ctypes.c_int),
-        "vd_set_schedule": ([vp, i64, ctypes.c_double], ctypes.c_int),
+        "vd_set_schedule": ([vp, i64, ctypes.c_double, ctypes.c_double], ctypes.c_int),
         "vd_set_tuning": ([vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "vd_profile": ([vp, dp, i64p, ctypes.c_int, ip], ctypes.c_int),
         "vd_profile_name": ([ctypes.c_int], ctypes.c_char_p),

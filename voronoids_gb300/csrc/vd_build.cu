@@ -194,54 +194,132 @@ __device__ __forceinline__ void write_hints(const DevTree& T, const vdp::VPt& q,
   for (int l = 0; l <= T.hint_levels; ++l) T.hint[hint_index<D>(T, q, l)] = slot;
 }
 
-// Priority-prefix histogram: prefix k holds the points with
-// thr[k-1] <= priority < thr[k].
+// Priority levels.  Level k holds the points with thr[k-1] <= priority <
+// thr[k]; the thresholds grow geometrically, so level sizes do too (the
+// biased randomized insertion order: every prefix of levels is a random
+// sample of the input).
 struct Thresholds {
-  unsigned long long t[kMaxPrefixes];
+  unsigned long long t[kMaxLevels];
   int n;
 };
 
-__global__ void k_prefix_hist(long long n, int base, unsigned long long seed, Thresholds th, int* counts) {
-  __shared__ int sh[kMaxPrefixes];
-  for (int k = threadIdx.x; k < kMaxPrefixes; k += blockDim.x) sh[k] = 0;
+__device__ __forceinline__ int level_of(unsigned long long pr, const unsigned long long* t, int n) {
+  int lo = 0, hi = n - 1;  // first k with pr < t[k]; t[n-1] = 2^32 holds every priority
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (pr < t[mid]) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+__global__ void k_level_hist(long long n, int base, unsigned long long seed, Thresholds th, int* counts) {
+  __shared__ int sh[kMaxLevels];
+  __shared__ unsigned long long st[kMaxLevels];
+  for (int k = threadIdx.x; k < kMaxLevels; k += blockDim.x) {
+    sh[k] = 0;
+    st[k] = th.t[k];
+  }
   __syncthreads();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const unsigned long long pr = priority((uint32_t)(base + i), seed);
-    int k = 0;
-    while (k < th.n - 1 && pr >= th.t[k]) ++k;
-    atomicAdd(&sh[k], 1);
-  }
+       i += (long long)gridDim.x * blockDim.x)
+    atomicAdd(&sh[level_of(priority((uint32_t)(base + i), seed), st, th.n)], 1);
   __syncthreads();
   for (int k = threadIdx.x; k < th.n; k += blockDim.x)
     if (sh[k]) atomicAdd(counts + k, sh[k]);
 }
 
-// Activates the points of one priority prefix: each walks from the finest
+// Level offsets (exclusive scan of the counts) and a fresh feed.
+__global__ void k_level_init(DevTree T, const int* counts, int nlev) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int acc = 0;
+  for (int k = 0; k < nlev; ++k) {
+    T.lev_off[k] = acc;
+    acc += counts[k];
+  }
+  for (int k = nlev; k <= kMaxLevels; ++k) T.lev_off[k] = acc;
+  T.ctr->lev_next = 0;
+  T.ctr->nlev = nlev;
+  T.ctr->feed_lo = 0;
+  T.ctr->feed_hi = 0;
+}
+
+// Scatter of the vertex ids into `order`, level by level.  Each tile of the
+// block ranks its items per level in shared memory and reserves one range
+// per level with a single global atomic.
+__global__ void k_level_order(DevTree T, long long n, int base, unsigned long long seed, Thresholds th,
+                              int* cursor) {
+  __shared__ int cnt[kMaxLevels], gb[kMaxLevels];
+  __shared__ unsigned long long st[kMaxLevels];
+  for (int k = threadIdx.x; k < kMaxLevels; k += blockDim.x) {
+    cnt[k] = 0;
+    st[k] = th.t[k];
+  }
+  __syncthreads();
+  for (long long b = blockIdx.x * (long long)blockDim.x; b < n; b += (long long)gridDim.x * blockDim.x) {
+    const long long i = b + threadIdx.x;
+    int lev = -1, rank = 0;
+    if (i < n) {
+      lev = level_of(priority((uint32_t)(base + i), seed), st, th.n);
+      rank = atomicAdd(&cnt[lev], 1);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < th.n; k += blockDim.x)
+      if (cnt[k]) gb[k] = atomicAdd(cursor + k, cnt[k]);
+    __syncthreads();
+    if (lev >= 0) T.order[T.lev_off[lev] + gb[lev] + rank] = base + (int)i;
+    __syncthreads();
+    for (int k = threadIdx.x; k < th.n; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+  }
+}
+
+// Feed decision of a round (one thread): levels are activated while fewer
+// than `ratio` x inserted points are active, and at least one level when no
+// point is active.  Keeping the active set proportional to the triangulation
+// keeps the share of points that win a round high, so few rounds are needed
+// and each point is located and nominated only a few times.
+__global__ void k_plan(DevTree T, int round, float ratio) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Counters* c = T.ctr;
+  long long a = c->nact[round & 1];
+  const double target = (double)ratio * (double)c->ninserted;
+  int lev = c->lev_next;
+  const int first = lev;
+  while (lev < c->nlev && (a == 0 || (double)a < target)) {
+    a += T.lev_off[lev + 1] - T.lev_off[lev];
+    ++lev;
+  }
+  c->feed_lo = T.lev_off[first];
+  c->feed_hi = T.lev_off[lev];
+  c->lev_next = lev;
+}
+
+// Activates the points planned for this round: each walks from the finest
 // available grid hint to the simplex that contains it (visibility walk,
 // exact orientation), joins the active list and votes for this round.
 template <int D>
-__global__ void k_activate(DevTree T, long long n, int base, unsigned long long seed,
-                           unsigned long long lo, unsigned long long hi, int round) {
+__global__ void k_activate(DevTree T, unsigned long long seed, int round) {
   constexpr int NV = D + 1;
   const int par = round & 1;
   const unsigned long long ep = epoch(round);
+  const int lo = T.ctr->feed_lo, n = T.ctr->feed_hi - lo;
   vdp::Tally tl = {0, 0, 0, 0};
   int perr = 0;
   unsigned long long walk = 0;
   const int cap = 1 << 16;
-  for (long long b = blockIdx.x * (long long)blockDim.x; b < n; b += (long long)gridDim.x * blockDim.x) {
-    const long long i = b + threadIdx.x;
-    bool act = false;
-    int cur = 0;
+  for (int b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+    const int i = b + threadIdx.x;
+    const bool act = i < n;
+    int cur = 0, vid = 0;
     unsigned pr = 0;
-    int vid = 0;
-    if (i < n) {
-      vid = base + (int)i;
-      pr = priority((uint32_t)vid, seed);
-      act = pr >= lo && pr < hi;
-    }
     if (act) {
+      vid = T.order[lo + i];
+      if (bad_vert(T, vid)) {
+        set_error(T.ctr, E_INTERNAL);
+        vid = 0;
+      }
+      pr = priority((uint32_t)vid, seed);
       const vdp::VPt p = load_pt(T, vid);
       cur = -1;
       for (int l = T.hint_levels; l >= 0 && cur < 0; --l) cur = T.hint[hint_index<D>(T, p, l)];
@@ -1127,7 +1205,7 @@ __global__ void k_relocate(DevTree T, int round) {
 }
 
 template <int D>
-void round_impl(const DevTree& T, const Launch& L, int round, const Tuning& tu, Prof* pf) {
+void round_impl(const DevTree& T, const Launch& L, int round, const Tuning& tu, const Feed& fd, Prof* pf) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_check<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * (int)sizeof(WarpCommit<D>));
@@ -1140,7 +1218,10 @@ void round_impl(const DevTree& T, const Launch& L, int round, const Tuning& tu, 
     }
   };
   if (pf && pf->n == 0) cudaEventRecord(pf->ev[0], L.stream);
-  note_launches(4 + 2 * tu.passes - 1);
+  note_launches(6 + 2 * tu.passes - 1);
+  k_plan<<<1, 32, 0, L.stream>>>(T, round, fd.ratio);
+  k_activate<D><<<L.blocks, 256, 0, L.stream>>>(T, fd.seed, round);
+  mark(KT_ACTIVATE);
   k_pick<<<L.blocks, 256, 0, L.stream>>>(T, round);
   mark(KT_PICK);
   k_thin<D><<<L.blocks, 256, 0, L.stream>>>(T, round, tu.thin);
@@ -1171,29 +1252,23 @@ void launch_upload(const DevTree& T, const Launch& L, int dim, const double* d_x
     k_upload<2><<<L.blocks, 256, 0, L.stream>>>(T, d_xyz, n, base_vid, sup);
 }
 
-void launch_prefix_hist(const Launch& L, int64_t n, int base_vid, uint64_t seed,
-                        const unsigned long long* thr, int nthr, int* d_counts) {
-  note_launches(1);
+void launch_levels(const DevTree& T, const Launch& L, int64_t n, int base_vid, uint64_t seed,
+                   const unsigned long long* thr, int nlev, int* d_work) {
+  note_launches(3);
   Thresholds th;
-  th.n = nthr;
-  for (int k = 0; k < kMaxPrefixes; ++k) th.t[k] = k < nthr ? thr[k] : ~0ull;
-  k_prefix_hist<<<L.blocks, 256, 0, L.stream>>>(n, base_vid, seed, th, d_counts);
+  th.n = nlev;
+  for (int k = 0; k < kMaxLevels; ++k) th.t[k] = k < nlev ? thr[k] : ~0ull;
+  k_level_hist<<<L.blocks, 256, 0, L.stream>>>(n, base_vid, seed, th, d_work);
+  k_level_init<<<1, 32, 0, L.stream>>>(T, d_work, nlev);
+  k_level_order<<<L.blocks, 256, 0, L.stream>>>(T, n, base_vid, seed, th, d_work + kMaxLevels);
 }
 
-void launch_activate(const DevTree& T, const Launch& L, int dim, int64_t n, int base_vid, uint64_t seed,
-                     unsigned long long lo, unsigned long long hi, int round) {
-  note_launches(1);
+void launch_round(const DevTree& T, const Launch& L, int dim, int round, const Tuning& tu, const Feed& fd,
+                  Prof* pf) {
   if (dim == 3)
-    k_activate<3><<<L.blocks, 256, 0, L.stream>>>(T, n, base_vid, seed, lo, hi, round);
+    round_impl<3>(T, L, round, tu, fd, pf);
   else
-    k_activate<2><<<L.blocks, 256, 0, L.stream>>>(T, n, base_vid, seed, lo, hi, round);
-}
-
-void launch_round(const DevTree& T, const Launch& L, int dim, int round, const Tuning& tu, Prof* pf) {
-  if (dim == 3)
-    round_impl<3>(T, L, round, tu, pf);
-  else
-    round_impl<2>(T, L, round, tu, pf);
+    round_impl<2>(T, L, round, tu, fd, pf);
 }
 
 const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_thin",     "k_cavity", "k_check",

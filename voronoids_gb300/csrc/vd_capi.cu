@@ -152,11 +152,12 @@ struct vd_tree {
   // device staging of host input points (one-shot host path)
   double* d_in = nullptr;
   int64_t cap_in = 0;
-  // insertion schedule (priority prefixes)
+  // insertion schedule: priority levels from `first_prefix` points growing
+  // by `growth`, fed while fewer than `ratio` x inserted points are active
   int64_t first_prefix = 64;
-  double growth = 4.0;
-  int* d_counts = nullptr;
-  int* h_counts = nullptr;
+  double growth = 1.25;
+  double ratio = 0.4;
+  int* d_counts = nullptr;     // 2 * kMaxLevels ints: level counts, cursors
   // profiling: per-kernel time from CUDA events on the tree's stream
   bool prof = false;
   std::vector<vd::Prof> profs;   // one event log per round of a chunk
@@ -180,7 +181,7 @@ vd::Launch launch_of(const vd_tree* t) {
 
 int cuda_status(cudaError_t e) { return e == cudaSuccess ? vd::E_OK : vd::E_CUDA; }
 
-constexpr int kChunkMax = 16;
+constexpr int kChunkMax = 8;
 
 vd::Prof* round_prof(vd_tree* t, int k) {
   if (!t->prof) return nullptr;
@@ -290,8 +291,10 @@ int ensure_points(vd_tree* t, int64_t n_new) {
     dfree(t->T.cinfo);
     dfree(t->T.wl[0]);
     dfree(t->T.wl[1]);
+    dfree(t->T.order);
     if (dalloc(&t->T.act[0], c) || dalloc(&t->T.act[1], c) || dalloc(&t->T.cand, c) ||
-        dalloc(&t->T.cinfo, c) || dalloc(&t->T.wl[0], c) || dalloc(&t->T.wl[1], c))
+        dalloc(&t->T.cinfo, c) || dalloc(&t->T.wl[0], c) || dalloc(&t->T.wl[1], c) ||
+        dalloc(&t->T.order, c))
       return vd::E_NOMEM;
     t->cap_act = c;
     t->T.cap_cand = (int)c;
@@ -329,6 +332,7 @@ void release(vd_tree* t) {
   dfree(t->T.killed);
   dfree(t->T.act[0]);
   dfree(t->T.act[1]);
+  dfree(t->T.order);
   dfree(t->T.cand);
   dfree(t->T.cinfo);
   dfree(t->T.wl[0]);
@@ -350,10 +354,9 @@ void release(vd_tree* t) {
   dfree(t->d_misc);
   dfree(t->d_loc);
   dfree(t->d_counts);
+  dfree(t->T.lev_off);
   dfree(t->T.hint);
   dfree(t->T.wchunk);
-  if (t->h_counts) cudaFreeHost(t->h_counts);
-  t->h_counts = nullptr;
   if (t->h_mm) cudaFreeHost(t->h_mm);
   t->h_mm = nullptr;
   dfree(t->d_in);
@@ -390,9 +393,9 @@ int alloc_tree(vd_tree* t, int dim, void* stream) {
   if (cudaMallocHost((void**)&t->h_pair, 16 * sizeof(int)) != cudaSuccess) return vd::E_NOMEM;
   memset(t->hctr, 0, sizeof(Counters));
   if (dalloc(&t->T.ctr, 1) || dalloc(&t->d_pair, 4) || dalloc(&t->d_check, 8) ||
-      dalloc(&t->d_misc, 16) || dalloc(&t->d_counts, vd::kMaxPrefixes))
+      dalloc(&t->d_misc, 16) || dalloc(&t->d_counts, 2 * vd::kMaxLevels) ||
+      dalloc(&t->T.lev_off, vd::kMaxLevels + 1))
     return vd::E_NOMEM;
-  if (cudaMallocHost((void**)&t->h_counts, sizeof(int) * vd::kMaxPrefixes) != cudaSuccess) return vd::E_NOMEM;
   if (cudaMallocHost((void**)&t->h_mm, 8 * sizeof(unsigned long long)) != cudaSuccess) return vd::E_NOMEM;
   t->T.cap_wchunk = t->sms * 20;
   if (dalloc(&t->T.wchunk, t->T.cap_wchunk)) return vd::E_NOMEM;
@@ -530,19 +533,29 @@ vd::Launch sized_launch(const vd_tree* t, int64_t items) {
   return L;
 }
 
-// Runs insertion rounds until at most `stop` points are still active.
-int run_rounds(vd_tree* t, const vd::Launch& L, int& r, int64_t stop) {
-  int chunk = 2;
+// Runs insertion rounds until every priority level of the current call has
+// been fed and no point is active.  The host only reads the counters between
+// chunks of rounds (to grow pools and to stop); within a chunk the feed is
+// decided on the device.
+int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
+  const vd::Feed fd{seed, (float)t->ratio};
+  int chunk = 1;
   int64_t last_progress = -1;
   int stalled = 0;
   int rc = vd::E_OK;
+  Counters& h = *t->hctr;
+  int64_t active = 0, fed = 0, done = t->hctr->ninserted;
   while (true) {
     if (t->trace) chunk = 1;
-    for (int k = 0; k < chunk; ++k) vd::launch_round(t->T, L, t->dim, r++, t->tuning, round_prof(t, k));
+    // grid sized for the most points that can be active during the chunk
+    const double grow = std::pow(1.4, chunk);
+    const int64_t est = std::min<int64_t>(n_call - fed + active,
+                                          (int64_t)((double)(done + active + 256) * grow));
+    const vd::Launch L = sized_launch(t, est);
+    for (int k = 0; k < chunk; ++k) vd::launch_round(t->T, L, t->dim, r++, t->tuning, fd, round_prof(t, k));
     rc = sync_counters(t);
     if (rc) break;
     accumulate_events(t, chunk);
-    Counters& h = *t->hctr;
     if (t->trace) {
       // GPU time of the round in microseconds when profiling is on
       int64_t us = -1;
@@ -565,7 +578,11 @@ int run_rounds(vd_tree* t, const vd::Launch& L, int& r, int64_t stop) {
       rc = h.err;
       break;
     }
-    if (h.nact[r & 1] <= stop) break;
+    active = h.nact[r & 1];
+    fed = h.feed_hi;
+    done = h.ninserted;
+    const bool all_fed = h.lev_next >= h.nlev;
+    if (all_fed && active == 0) break;
     // grow pools when a round had to defer work
     bool fix = false;
     if (h.simp_overflow || (double)h.nsimp > 0.85 * t->T.cap_simp) {
@@ -599,17 +616,17 @@ int run_rounds(vd_tree* t, const vd::Launch& L, int& r, int64_t stop) {
       stalled = 0;
       last_progress = progress;
     }
-    chunk = std::min(chunk * 2, kChunkMax);
+    // once everything is fed the active set drains in a few rounds
+    chunk = all_fed ? 2 : std::min(chunk * 2, kChunkMax);
   }
   return rc;
 }
 
-// Insertion of n points already in device memory.  Points are inserted in
-// priority prefixes (first `first_prefix` points, then geometrically growing
-// by `growth`): only the points of the current prefix are located, relocated
-// and nominated, so early rounds, which can only insert a few points into a
-// small triangulation, do not pay for the whole input.  Each prefix is
-// located by walks from the hint grid and then inserted in rounds.
+// Insertion of n points already in device memory.  The points are split into
+// priority levels (the first `first_prefix` points, then growing by
+// `growth`); rounds activate levels as the triangulation grows (k_plan), so
+// early rounds, which can only insert a few points into a small
+// triangulation, do not locate, relocate or nominate the whole input.
 int insert_device(vd_tree* t, const double* d_xyz, int64_t n, uint64_t seed) {
   if (n < 0 || (n > 0 && !d_xyz)) return vd::E_ARG;
   if (n == 0) return vd::E_OK;
@@ -622,46 +639,26 @@ int insert_device(vd_tree* t, const double* d_xyz, int64_t n, uint64_t seed) {
   const vd::Launch L = launch_of(t);
   const int base = (int)t->nverts;
   vd::launch_upload(t->T, L, t->dim, d_xyz, n, base, t->sup_order);
-  // priority thresholds of the prefixes
   std::vector<unsigned long long> thr;
   {
     double m = std::min<double>((double)std::max<int64_t>(t->first_prefix, 1), (double)n);
-    const unsigned long long top = 1ull << 32;
-    while ((int)thr.size() < vd::kMaxPrefixes - 1) {
+    while ((int)thr.size() < vd::kMaxLevels - 1) {
       const double f = m / (double)n;
       if (f >= 1.0) break;
       thr.push_back((unsigned long long)(f * 4294967296.0));
-      m *= std::max(1.5, t->growth);
+      m = std::max(m * t->growth, m + 1.0);
     }
-    thr.push_back(top);
+    thr.push_back(1ull << 32);
   }
-  cudaMemsetAsync(t->d_counts, 0, sizeof(int) * vd::kMaxPrefixes, t->stream);
-  vd::launch_prefix_hist(L, n, base, seed, thr.data(), (int)thr.size(), t->d_counts);
-  cudaMemcpyAsync(t->h_counts, t->d_counts, sizeof(int) * vd::kMaxPrefixes, cudaMemcpyDeviceToHost, t->stream);
+  cudaMemsetAsync(t->d_counts, 0, sizeof(int) * 2 * vd::kMaxLevels, t->stream);
+  vd::launch_levels(t->T, L, n, base, seed, thr.data(), (int)thr.size(), t->d_counts);
   rc = sync_counters(t);
   if (rc) return rc;
   if (t->hctr->err) return t->hctr->err;
   t->nverts += n;
   t->calls++;
   int r = t->round;
-  // The next prefix is activated once the current one is down to its tail
-  // (a tenth of it), so the tail's rounds also insert the next prefix.
-  int last = -1;
-  for (size_t k = 0; k < thr.size(); ++k)
-    if (t->h_counts[k] > 0) last = (int)k;
-  int64_t carried = 0;
-  for (size_t k = 0; k < thr.size() && !rc; ++k) {
-    const int cnt = t->h_counts[k];
-    if (cnt == 0) continue;
-    const unsigned long long lo = k ? thr[k - 1] : 0ull;
-    {
-      ScopedProf sp(t, vd::KT_ACTIVATE);
-      vd::launch_activate(t->T, L, t->dim, n, base, seed, lo, thr[k], r);
-    }
-    const int64_t stop = (int)k == last ? 0 : cnt / 10;
-    rc = run_rounds(t, sized_launch(t, cnt + carried), r, stop);
-    carried = t->hctr->nact[r & 1];
-  }
+  rc = run_rounds(t, r, n, seed);
   t->round = r;
   vd::launch_close_chunks(t->T, L);
   if (!rc) rc = sync_counters(t);
@@ -1089,10 +1086,12 @@ const char* vd_profile_name(int i) {
   return "";
 }
 
-int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth) {
-  if (ready(t) || first_prefix < 1 || !(growth >= 1.5)) return VD_ERR_ARG;
+int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth, double ratio) {
+  if (ready(t) || first_prefix < 1 || !(growth > 1.0 && growth <= 16.0) || !(ratio > 0.0 && ratio <= 64.0))
+    return VD_ERR_ARG;
   t->first_prefix = first_prefix;
   t->growth = growth;
+  t->ratio = ratio;
   return VD_OK;
 }
 

@@ -87,10 +87,15 @@ struct Counters {
   unsigned long long won[kPassesMax];  // winners per resolution pass
   unsigned long long spilled;       // searches that used the pool spill path
   int nwl[kStages];                 // work-list lengths of the current round
+  // continuous feed of priority levels (see k_plan in vd_build.cu)
+  int lev_next;                     // first level not yet activated
+  int nlev;                         // levels of the current call
+  int feed_lo, feed_hi;             // range of `order` activated this round
 };
 
-// Insertion proceeds in priority prefixes (see vd_capi.cu); at most this many.
-constexpr int kMaxPrefixes = 48;
+// Points of one insertion call are split into priority levels of
+// geometrically growing size; at most this many.
+constexpr int kMaxLevels = 96;
 
 struct DevTree {
   vdp::VPt* pts;
@@ -111,6 +116,8 @@ struct DevTree {
   Counters* ctr;
   int2* wchunk;       // per-warp fresh-slot chunk (base, left) of k_check
   int cap_wchunk;
+  int* order;         // vertex ids of the current call grouped by priority level
+  int* lev_off;       // kMaxLevels + 1 offsets of the levels in `order`
   int* hint;          // location hints, levels 0..hint_levels (see vd_build.cu)
   int hint_levels;
   double gorg[3];     // hint grid origin and 1 / extent
@@ -168,10 +175,20 @@ struct Launch {
 
 void launch_upload(const DevTree& T, const Launch& L, int dim, const double* d_xyz, int64_t n,
                    int base_vid, const int* super_order);
-void launch_prefix_hist(const Launch& L, int64_t n, int base_vid, uint64_t seed,
-                        const unsigned long long* thr, int nthr, int* d_counts);
-void launch_activate(const DevTree& T, const Launch& L, int dim, int64_t n, int base_vid, uint64_t seed,
-                     unsigned long long lo, unsigned long long hi, int round);
+// Priority levels of the points base_vid .. base_vid + n - 1: level k holds
+// the priorities in [thr[k-1], thr[k]).  d_work holds 2 * kMaxLevels ints
+// (counts, cursors) and must be zero on entry; on exit T.order lists the
+// points level by level, T.lev_off[0..nlev] bounds the levels and the feed
+// counters are reset to level 0.
+void launch_levels(const DevTree& T, const Launch& L, int64_t n, int base_vid, uint64_t seed,
+                   const unsigned long long* thr, int nlev, int* d_work);
+// Feed of one round: activate priority levels while the active points are
+// fewer than `ratio` times the inserted ones (at least one level when none
+// is active).
+struct Feed {
+  uint64_t seed;
+  float ratio;
+};
 // Runtime tuning of a round: resolution passes (1..kPassesMax) and the
 // thinning radius (1: face neighbours, 2: also their neighbours).
 struct Tuning {
@@ -189,7 +206,8 @@ struct Prof {
   int type[kMax];
   int n;
 };
-void launch_round(const DevTree& T, const Launch& L, int dim, int round, const Tuning& tu, Prof* pf);
+void launch_round(const DevTree& T, const Launch& L, int dim, int round, const Tuning& tu, const Feed& fd,
+                  Prof* pf);
 
 // Edges: counts / offsets / segment buffers are caller-provided device arrays.
 struct EdgeScratch {

@@ -172,8 +172,9 @@ class DelaunayTree:
                                    n.value, ctypes.byref(n)), "duplicates")
         return out
 
-    def set_schedule(self, first_prefix=64, growth=4.0):
-        _check(_native.load().vd_set_schedule(self._h, int(first_prefix), float(growth)), "set_schedule")
+    def set_schedule(self, first_prefix=64, growth=1.25, ratio=0.4):
+        _check(_native.load().vd_set_schedule(self._h, int(first_prefix), float(growth), float(ratio)),
+               "set_schedule")
 
     def set_tuning(self, passes=3, thin=1):
         _check(_native.load().vd_set_tuning(self._h, int(passes), int(thin)), "set_tuning")
