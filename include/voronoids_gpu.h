@@ -161,12 +161,16 @@ int vd_set_profiling(vd_tree* t, int on);
  * of a call are split by priority into levels of `first_prefix` points, then
  * growing by `growth` (1 < growth <= 16); a round activates further levels
  * while fewer than `ratio` (0 < ratio <= 64) times the inserted points are
- * active.  Defaults 64, 1.25 and 0.4. */
+ * active.  Defaults 64, 1.25 and 0.12. */
 int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth, double ratio);
 /* Round tuning: resolution passes per round (1..6) and the thinning radius
  * (1 = a nominee must hold its simplex and face neighbours, 2 = and no lower
  * nominee two faces away).  Defaults: 3D 2 passes / radius 2, 2D 3 / 1. */
 int vd_set_tuning(vd_tree* t, int passes, int thin);
+/* Rounds are launched in chunks captured once as CUDA graphs and replayed
+ * (default on; profiling and tracing launch kernel by kernel).  No reference
+ * counterpart. */
+int vd_set_graphs(vd_tree* t, int on);
 int vd_profile(vd_tree* t, double* ms, int64_t* launches, int cap, int* n);
 const char* vd_profile_name(int i);
 int vd_set_trace(vd_tree* t, int on);

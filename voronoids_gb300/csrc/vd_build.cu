@@ -279,9 +279,11 @@ __global__ void k_level_order(DevTree T, long long n, int base, unsigned long lo
 // point is active.  Keeping the active set proportional to the triangulation
 // keeps the share of points that win a round high, so few rounds are needed
 // and each point is located and nominated only a few times.
-__global__ void k_plan(DevTree T, int round, float ratio) {
+__global__ void k_plan(DevTree T, float ratio) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   Counters* c = T.ctr;
+  const int round = c->round + 1;  // the round this launch opens
+  c->round = round;
   long long a = c->nact[round & 1];
   const double target = (double)ratio * (double)c->ninserted;
   int lev = c->lev_next;
@@ -299,7 +301,8 @@ __global__ void k_plan(DevTree T, int round, float ratio) {
 // available grid hint to the simplex that contains it (visibility walk,
 // exact orientation), joins the active list and votes for this round.
 template <int D>
-__global__ void k_activate(DevTree T, unsigned long long seed, int round) {
+__global__ void k_activate(DevTree T, unsigned long long seed) {
+  const int round = T.ctr->round;
   constexpr int NV = D + 1;
   const int par = round & 1;
   const unsigned long long ep = epoch(round);
@@ -365,7 +368,8 @@ __global__ void k_activate(DevTree T, unsigned long long seed, int round) {
 }
 
 // ---------------------------------------------------------------------------
-__global__ void k_pick(DevTree T, int round) {
+__global__ void k_pick(DevTree T) {
+  const int round = T.ctr->round;
   const int par = round & 1;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     T.ctr->nact[par ^ 1] = 0;
@@ -567,7 +571,8 @@ __device__ bool thin_lost1(const DevTree& T, int home, int4 n0, unsigned long lo
 // Per nominee (one thread): duplicate test against the vertices of its
 // simplex and the thinning test; survivors go to work list stage 0.
 template <int D>
-__global__ void k_thin(DevTree T, int round, int thin) {
+__global__ void k_thin(DevTree T, int thin) {
+  const int round = T.ctr->round;
   constexpr int NV = D + 1;
   const int nc = min(T.ctr->ncand, T.cap_cand);
   const unsigned long long ep = epoch(round);
@@ -623,7 +628,8 @@ __device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int
 }
 
 template <int D>
-__global__ void __launch_bounds__(128) k_cavity(DevTree T, int round) {
+__global__ void __launch_bounds__(128) k_cavity(DevTree T) {
+  const int round = T.ctr->round;
   constexpr int MAXC = Cap<D>::MAXC, MAXF = Cap<D>::MAXF, HS = Cap<D>::HS;
   __shared__ WarpCav<D> smem[4];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -937,7 +943,8 @@ __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, i
 // the slot of k when it is the first facet of k, so a point that was inside
 // k usually finds itself in (or next to) the simplex now in k's slot.
 template <int D>
-__global__ void __launch_bounds__(128) k_check(DevTree T, int round, int pass, int last) {
+__global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last) {
+  const int round = T.ctr->round;
   const int sin = 2 * pass, sout = 2 * pass + 1;
   constexpr int MAXF = Cap<D>::MAXF, MAXC = Cap<D>::MAXC;
   extern __shared__ __align__(16) unsigned char dsm[];
@@ -1092,7 +1099,8 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int round, int pass, i
 // neighbour a winner removed, drops out for this round; the others claim
 // again with this pass's key (smaller than every earlier key of the round).
 template <int D>
-__global__ void __launch_bounds__(128) k_reclaim(DevTree T, int round, int pass) {
+__global__ void __launch_bounds__(128) k_reclaim(DevTree T, int pass) {
+  const int round = T.ctr->round;
   const int sin = 2 * pass - 1, sout = 2 * pass;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nc = min(T.ctr->ncand, T.cap_cand);
@@ -1129,7 +1137,8 @@ __global__ void __launch_bounds__(128) k_reclaim(DevTree T, int round, int pass)
 }
 
 template <int D>
-__global__ void k_relocate(DevTree T, int round) {
+__global__ void k_relocate(DevTree T) {
+  const int round = T.ctr->round;
   constexpr int NV = D + 1;
   const int par = round & 1;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1205,12 +1214,7 @@ __global__ void k_relocate(DevTree T, int round) {
 }
 
 template <int D>
-void round_impl(const DevTree& T, const Launch& L, int round, const Tuning& tu, const Feed& fd, Prof* pf) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_check<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * (int)sizeof(WarpCommit<D>));
-    attr = true;
-  }
+void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed& fd, Prof* pf) {
   auto mark = [&](int type) {
     if (pf && pf->n < Prof::kMax) {
       cudaEventRecord(pf->ev[pf->n + 1], L.stream);
@@ -1219,24 +1223,24 @@ void round_impl(const DevTree& T, const Launch& L, int round, const Tuning& tu, 
   };
   if (pf && pf->n == 0) cudaEventRecord(pf->ev[0], L.stream);
   note_launches(6 + 2 * tu.passes - 1);
-  k_plan<<<1, 32, 0, L.stream>>>(T, round, fd.ratio);
-  k_activate<D><<<L.blocks, 256, 0, L.stream>>>(T, fd.seed, round);
+  k_plan<<<1, 32, 0, L.stream>>>(T, fd.ratio);
+  k_activate<D><<<L.blocks, 256, 0, L.stream>>>(T, fd.seed);
   mark(KT_ACTIVATE);
-  k_pick<<<L.blocks, 256, 0, L.stream>>>(T, round);
+  k_pick<<<L.blocks, 256, 0, L.stream>>>(T);
   mark(KT_PICK);
-  k_thin<D><<<L.blocks, 256, 0, L.stream>>>(T, round, tu.thin);
+  k_thin<D><<<L.blocks, 256, 0, L.stream>>>(T, tu.thin);
   mark(KT_THIN);
-  k_cavity<D><<<L.warps / 4, 128, 0, L.stream>>>(T, round);
+  k_cavity<D><<<L.warps / 4, 128, 0, L.stream>>>(T);
   mark(KT_CAVITY);
   for (int p = 0; p < tu.passes; ++p) {
     if (p > 0) {
-      k_reclaim<D><<<L.warps / 4, 128, 0, L.stream>>>(T, round, p);
+      k_reclaim<D><<<L.warps / 4, 128, 0, L.stream>>>(T, p);
       mark(KT_RECLAIM);
     }
-    k_check<D><<<L.warps / 4, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, round, p, p == tu.passes - 1);
+    k_check<D><<<L.warps / 4, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, p == tu.passes - 1);
     mark(KT_CHECK);
   }
-  k_relocate<D><<<L.blocks, 256, 0, L.stream>>>(T, round);
+  k_relocate<D><<<L.blocks, 256, 0, L.stream>>>(T);
   mark(KT_RELOCATE);
 }
 
@@ -1263,12 +1267,19 @@ void launch_levels(const DevTree& T, const Launch& L, int64_t n, int base_vid, u
   k_level_order<<<L.blocks, 256, 0, L.stream>>>(T, n, base_vid, seed, th, d_work + kMaxLevels);
 }
 
-void launch_round(const DevTree& T, const Launch& L, int dim, int round, const Tuning& tu, const Feed& fd,
-                  Prof* pf) {
+int prepare_round_kernels() {
+  const cudaError_t e3 = cudaFuncSetAttribute(k_check<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              4 * (int)sizeof(WarpCommit<3>));
+  const cudaError_t e2 = cudaFuncSetAttribute(k_check<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              4 * (int)sizeof(WarpCommit<2>));
+  return e3 == cudaSuccess && e2 == cudaSuccess ? E_OK : E_CUDA;
+}
+
+void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, const Feed& fd, Prof* pf) {
   if (dim == 3)
-    round_impl<3>(T, L, round, tu, fd, pf);
+    round_impl<3>(T, L, tu, fd, pf);
   else
-    round_impl<2>(T, L, round, tu, fd, pf);
+    round_impl<2>(T, L, tu, fd, pf);
 }
 
 const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_thin",     "k_cavity", "k_check",

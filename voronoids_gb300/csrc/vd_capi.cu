@@ -156,7 +156,7 @@ struct vd_tree {
   // by `growth`, fed while fewer than `ratio` x inserted points are active
   int64_t first_prefix = 64;
   double growth = 1.25;
-  double ratio = 0.4;
+  double ratio = 0.12;
   int* d_counts = nullptr;     // 2 * kMaxLevels ints: level counts, cursors
   // profiling: per-kernel time from CUDA events on the tree's stream
   bool prof = false;
@@ -167,6 +167,18 @@ struct vd_tree {
   // per-round trace (diagnostics; syncs after every round)
   bool trace = false;
   std::vector<int64_t> trace_rows;
+  // chunks of rounds captured as CUDA graphs, keyed by everything a launch
+  // bakes in (the device tree by value, grid, tuning and feed)
+  struct ChunkGraph {
+    vd::DevTree T;
+    int chunk, blocks, warps, passes, thin;
+    uint64_t seed;
+    float ratio;
+    long long launches;
+    cudaGraphExec_t exec;
+  };
+  std::vector<ChunkGraph> graphs;
+  bool use_graphs = true;
 };
 
 namespace {
@@ -318,7 +330,13 @@ int ensure_points(vd_tree* t, int64_t n_new) {
   return vd::E_OK;
 }
 
+void drop_graphs(vd_tree* t) {
+  for (auto& g : t->graphs) cudaGraphExecDestroy(g.exec);
+  t->graphs.clear();
+}
+
 void release(vd_tree* t) {
+  drop_graphs(t);
   if (!t) return;
   if (t->stream) cudaStreamSynchronize(t->stream);
   dfree(t->T.pts);
@@ -382,6 +400,7 @@ int alloc_tree(vd_tree* t, int dim, void* stream) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   t->sms = std::max(sms, 1);
+  if (vd::prepare_round_kernels() != vd::E_OK) return vd::E_CUDA;
   if (stream) {
     t->stream = (cudaStream_t)stream;
     t->own_stream = false;
@@ -461,6 +480,7 @@ int set_geometry(vd_tree* t, const double* c, double rb) {
   cudaMemcpyAsync(t->T.simp, &t->h_s0, sizeof(vd::Simplex), cudaMemcpyHostToDevice, t->stream);
   memset(t->hctr, 0, sizeof(Counters));
   t->hctr->nsimp = 1;
+  t->hctr->round = t->round - 1;  // the next k_plan opens round t->round
   cudaMemcpyAsync(t->T.ctr, t->hctr, sizeof(Counters), cudaMemcpyHostToDevice, t->stream);
   return cuda_status(cudaStreamSynchronize(t->stream));
 }
@@ -526,11 +546,70 @@ int size_from_device(vd_tree* t, const double* d_pts, int64_t n, double* c, doub
 
 vd::Launch sized_launch(const vd_tree* t, int64_t items) {
   vd::Launch L = launch_of(t);
+  int64_t p2 = 128;  // powers of two keep the set of captured grids small
+  while (p2 < items) p2 <<= 1;
+  items = p2;
   const int64_t blocks = (items + 255) / 256;
   L.blocks = (int)std::max<int64_t>(1, std::min<int64_t>(blocks, L.blocks));
   const int64_t warps = ((items + 3) / 4) * 4;
   L.warps = (int)std::max<int64_t>(4, std::min<int64_t>(warps, L.warps));
   return L;
+}
+
+// Launches `chunk` rounds as one CUDA graph, capturing it on first use.
+// Returns false (nothing launched) when graphs are off for this tree:
+// profiling and tracing need per-kernel events, and a failed capture turns
+// graphs off.
+bool launch_chunk_graph(vd_tree* t, const vd::Launch& L, int chunk, const vd::Feed& fd) {
+  if (!t->use_graphs || t->prof || t->trace) return false;
+  vd_tree::ChunkGraph* hit = nullptr;
+  for (auto& g : t->graphs)
+    if (g.chunk == chunk && g.blocks == L.blocks && g.warps == L.warps && g.passes == t->tuning.passes &&
+        g.thin == t->tuning.thin && g.seed == fd.seed && g.ratio == fd.ratio &&
+        memcmp(&g.T, &t->T, sizeof(vd::DevTree)) == 0) {
+      hit = &g;
+      break;
+    }
+  if (!hit) {
+    if (t->graphs.size() >= 24) drop_graphs(t);
+    const long long before = vd::launches_total();
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool ok = cudaStreamBeginCapture(t->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      for (int k = 0; k < chunk; ++k) vd::launch_round(t->T, L, t->dim, t->tuning, fd, nullptr);
+      ok = cudaStreamEndCapture(t->stream, &graph) == cudaSuccess && graph;
+    }
+    if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    const long long launches = vd::launches_total() - before;
+    vd::note_launches(-launches);  // counted when replayed
+    if (!ok) {
+      cudaGetLastError();
+      t->use_graphs = false;
+      return false;
+    }
+    vd_tree::ChunkGraph g;
+    memcpy(&g.T, &t->T, sizeof(vd::DevTree));
+    g.chunk = chunk;
+    g.blocks = L.blocks;
+    g.warps = L.warps;
+    g.passes = t->tuning.passes;
+    g.thin = t->tuning.thin;
+    g.seed = fd.seed;
+    g.ratio = fd.ratio;
+    g.launches = launches;
+    g.exec = exec;
+    t->graphs.push_back(g);
+    hit = &t->graphs.back();
+  }
+  if (cudaGraphLaunch(hit->exec, t->stream) != cudaSuccess) {
+    cudaGetLastError();
+    t->use_graphs = false;
+    return false;
+  }
+  vd::note_launches(hit->launches);
+  return true;
 }
 
 // Runs insertion rounds until every priority level of the current call has
@@ -552,7 +631,9 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
     const int64_t est = std::min<int64_t>(n_call - fed + active,
                                           (int64_t)((double)(done + active + 256) * grow));
     const vd::Launch L = sized_launch(t, est);
-    for (int k = 0; k < chunk; ++k) vd::launch_round(t->T, L, t->dim, r++, t->tuning, fd, round_prof(t, k));
+    if (!launch_chunk_graph(t, L, chunk, fd))
+      for (int k = 0; k < chunk; ++k) vd::launch_round(t->T, L, t->dim, t->tuning, fd, round_prof(t, k));
+    r += chunk;
     rc = sync_counters(t);
     if (rc) break;
     accumulate_events(t, chunk);
@@ -1099,6 +1180,13 @@ int vd_set_tuning(vd_tree* t, int passes, int thin) {
   if (ready(t) || passes < 1 || passes > vd::kPassesMax || thin < 1 || thin > 2) return VD_ERR_ARG;
   t->tuning.passes = passes;
   t->tuning.thin = thin;
+  return VD_OK;
+}
+
+int vd_set_graphs(vd_tree* t, int on) {
+  if (ready(t)) return VD_ERR_ARG;
+  t->use_graphs = on != 0;
+  if (!on) drop_graphs(t);
   return VD_OK;
 }
 

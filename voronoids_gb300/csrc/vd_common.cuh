@@ -91,6 +91,7 @@ struct Counters {
   int lev_next;                     // first level not yet activated
   int nlev;                         // levels of the current call
   int feed_lo, feed_hi;             // range of `order` activated this round
+  int round;                        // round being run (advanced by k_plan)
 };
 
 // Points of one insertion call are split into priority levels of
@@ -206,8 +207,13 @@ struct Prof {
   int type[kMax];
   int n;
 };
-void launch_round(const DevTree& T, const Launch& L, int dim, int round, const Tuning& tu, const Feed& fd,
-                  Prof* pf);
+// Kernel attributes the rounds need (shared-memory size); once per device
+// before the first round or capture.
+int prepare_round_kernels();
+// One insertion round; its number is kept on the device (Counters::round,
+// advanced by the round's first kernel), so a captured sequence of rounds
+// can be replayed.
+void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, const Feed& fd, Prof* pf);
 
 // Edges: counts / offsets / segment buffers are caller-provided device arrays.
 struct EdgeScratch {

@@ -172,12 +172,15 @@ class DelaunayTree:
                                    n.value, ctypes.byref(n)), "duplicates")
         return out
 
-    def set_schedule(self, first_prefix=64, growth=1.25, ratio=0.4):
+    def set_schedule(self, first_prefix=64, growth=1.25, ratio=0.12):
         _check(_native.load().vd_set_schedule(self._h, int(first_prefix), float(growth), float(ratio)),
                "set_schedule")
 
     def set_tuning(self, passes=3, thin=1):
         _check(_native.load().vd_set_tuning(self._h, int(passes), int(thin)), "set_tuning")
+
+    def set_graphs(self, on=True):
+        _check(_native.load().vd_set_graphs(self._h, int(on)), "set_graphs")
 
     def set_profiling(self, on=True):
         _check(_native.load().vd_set_profiling(self._h, int(on)), "set_profiling")
