@@ -191,6 +191,28 @@ int vd_delaunay_tree(vd_tree* t, const double* pts, int64_t n, uint64_t seed, ui
 int vd_delaunay_device(vd_tree* t, const double* d_pts, int64_t n, uint64_t seed, uint32_t* d_uv,
                        int64_t cap, int64_t* n_edges);
 
+/* Batched build (no reference counterpart: the reference builds one tree per
+ * call, src/lib.rs:104-125).  `nsets` independent point sets, set s being the
+ * points offsets[s] .. offsets[s+1]-1 of `pts` (offsets: nsets + 1 host
+ * entries, offsets[0] = 0, every set non-empty), are triangulated together in
+ * one pass of insertion rounds; each set's triangulation is exactly the one
+ * vd_delaunay builds for it alone with the same seed.  Edges are written set
+ * after set as uint32 pairs of point numbers within the set (u < v, sorted);
+ * edge_offsets (nsets + 1 host entries) bounds each set's edges.  The tree is
+ * reset to the batch (any earlier content is dropped); vd_check_delaunay,
+ * vd_get_stats and vd_num_edges (global numbering) then apply to all sets.
+ * Host points in, host pairs out: */
+int vd_batch_delaunay(vd_tree* t, const double* pts, const int64_t* offsets, int nsets, uint64_t seed,
+                      uint32_t* uv, int64_t cap, int64_t* edge_offsets);
+/* Device points in, device pairs out (`offsets` and `edge_offsets` on the host). */
+int vd_batch_delaunay_device(vd_tree* t, const double* d_pts, const int64_t* offsets, int nsets, uint64_t seed,
+                             uint32_t* d_uv, int64_t cap, int64_t* edge_offsets);
+/* Point sets of the tree (1 unless built by vd_batch_*). */
+int vd_num_sets(vd_tree* t, int* nsets);
+/* An empty tree (no super simplex yet) for the batched calls, vd_tree_reset
+ * or vd_delaunay_tree / vd_delaunay_device. */
+vd_tree* vd_tree_create(int dim, void* stream, int* status);
+
 /* Sorted edge list of a caller-owned simplex list, for callers that may not
  * allocate GPU memory (for example an application whose memory manager owns
  * the whole device, or a loop that cannot afford the synchronisation of a

@@ -177,3 +177,19 @@ def test_c2_full_size_properties(vd):
     assert 7.4 < len(e) / n < 7.9
     # Euler: for a triangulated ball V - E + F - T = 1 over all simplices
     assert st["live_simplices"] == 1 + st["created"] - st["killed"]
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_reused_tree_matches_fresh(vd, oracle, dim):
+    # a tree reset for new points must show nothing of its earlier build
+    a = W.uniform_points(30000, dim, 61)
+    b = W.uniform_points(12000, dim, 62)
+    t = vd.DelaunayTree(a)
+    t.add_points_to_tree(a, seed=1)
+    for pts, seed in ((b, 2), (a, 3), (b, 4)):
+        t.reset(pts)
+        t.add_points_to_tree(pts, seed=seed)
+        ok, det = t.check_delaunay(details=True)
+        assert ok, det
+        assert np.array_equal(t.edges(), oracle.Triangulation(pts, seed=seed).edges())
+    t.close()

@@ -26,6 +26,7 @@ EXPORTS = [
     "vd_max_simplex_id", "vd_num_simplices", "vd_simplices", "vd_num_edges", "vd_edges",
     "vd_edges_device", "vd_check_delaunay", "vd_duplicates", "vd_get_stats", "vd_status_str",
     "vd_delaunay", "vd_set_schedule", "vd_set_tuning", "vd_set_graphs", "vd_set_profiling", "vd_profile", "vd_profile_name", "vd_set_trace", "vd_trace", "vd_kernel_launches", "vd_edges_from_simplices_noalloc",
+    "vd_batch_delaunay", "vd_batch_delaunay_device", "vd_num_sets", "vd_tree_create",
 ]
 
 
@@ -85,6 +86,10 @@ def load(path=LIB_PATH):
         "vd_set_schedule": ([vp, i64, ctypes.c_double, ctypes.c_double], ctypes.c_int),
         "vd_set_tuning": ([vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "vd_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
+        "vd_batch_delaunay": ([vp, dp, i64p, ctypes.c_int, ctypes.c_uint64, vp, i64, i64p], ctypes.c_int),
+        "vd_batch_delaunay_device": ([vp, vp, i64p, ctypes.c_int, ctypes.c_uint64, vp, i64, i64p], ctypes.c_int),
+        "vd_num_sets": ([vp, ip], ctypes.c_int),
+        "vd_tree_create": ([ctypes.c_int, vp, ip], vp),
         "vd_profile": ([vp, dp, i64p, ctypes.c_int, ip], ctypes.c_int),
         "vd_profile_name": ([ctypes.c_int], ctypes.c_char_p),
         "vd_set_trace": ([vp, ctypes.c_int], ctypes.c_int),

@@ -145,16 +145,21 @@ __device__ __forceinline__ int warp_append(int* counter, bool flag) {
 
 // ---------------------------------------------------------------------------
 template <int D>
-__global__ void k_upload(DevTree T, const double* xyz, long long n, int base, int4 sup) {
+__global__ void k_upload(DevTree T, const double* xyz, long long n, int base) {
   constexpr int NV = D + 1;
   const double lo = 7.006492321624085e-46;  // 2^-150
   const double hi = 1.4272476927059599e45;  // 2^150
   vdp::Tally tl = {0, 0, 0, 0};
   int perr = 0;
   vdp::VPt sv[NV];
-  for (int j = 0; j < NV; ++j) sv[j] = load_pt(T, get4(sup, j));
+  int cur_set = -1;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
+    const int set = set_index(T, base + (int)i);
+    if (set != cur_set) {  // super simplex of the point's set
+      cur_set = set;
+      for (int j = 0; j < NV; ++j) sv[j] = load_pt(T, T.sets[set].sup[j]);
+    }
     double c[3] = {xyz[i * D], xyz[i * D + 1], D == 3 ? xyz[i * D + 2] : 0.0};
     for (int k = 0; k < 3; ++k) {
       double a = fabs(c[k]);
@@ -169,29 +174,30 @@ __global__ void k_upload(DevTree T, const double* xyz, long long n, int base, in
   if (perr) set_error(T.ctr, E_PRECISION);
 }
 
-// Multi-level grid of location hints.  Level l splits the sizing box
-// (centre +- bounding radius) into 2^l cells per axis; each cell keeps the
-// slot of a simplex created near it (written by every winner, races are
-// harmless: any live simplex is a valid walk start, a near one is a short
-// walk).
+// Multi-level grid of location hints, one per set.  Level l splits the
+// set's sizing box (centre +- bounding radius) into 2^l cells per axis; each
+// cell keeps the slot of a simplex created near it (written by every winner,
+// races are harmless: any live simplex of the set is a valid walk start, a
+// near one is a short walk).
 template <int D>
-__device__ __forceinline__ int hint_index(const DevTree& T, const vdp::VPt& p, int level) {
+__device__ __forceinline__ int hint_index(const SetGeo& g, const vdp::VPt& p, int level) {
   const int side = 1 << level;
   const double c[3] = {p.x, p.y, p.z};
   int idx = 0;
   for (int k = D - 1; k >= 0; --k) {
-    double u = (c[k] - T.gorg[k]) * T.gscale;
+    double u = (c[k] - g.org[k]) * g.scale;
     int i = (int)(u * side);
     i = i < 0 ? 0 : (i >= side ? side - 1 : i);
     idx = idx * side + i;
   }
   const int off = D == 3 ? ((1 << (3 * level)) - 1) / 7 : ((1 << (2 * level)) - 1) / 3;
-  return off + idx;
+  return g.hint_off + off + idx;
 }
 
 template <int D>
-__device__ __forceinline__ void write_hints(const DevTree& T, const vdp::VPt& q, int slot) {
-  for (int l = 0; l <= T.hint_levels; ++l) T.hint[hint_index<D>(T, q, l)] = slot;
+__device__ __forceinline__ void write_hints(const DevTree& T, int vid, const vdp::VPt& q, int slot) {
+  const SetGeo& g = T.sets[set_index(T, vid)];
+  for (int l = 0; l <= g.hint_levels; ++l) T.hint[hint_index<D>(g, q, l)] = slot;
 }
 
 // Priority levels.  Level k holds the points with thr[k-1] <= priority <
@@ -201,6 +207,8 @@ __device__ __forceinline__ void write_hints(const DevTree& T, const vdp::VPt& q,
 struct Thresholds {
   unsigned long long t[kMaxLevels];
   int n;
+  double first;   // per-set levels (batched build): first level size
+  double lgrow;   // and log of the growth factor
 };
 
 __device__ __forceinline__ int level_of(unsigned long long pr, const unsigned long long* t, int n) {
@@ -213,7 +221,17 @@ __device__ __forceinline__ int level_of(unsigned long long pr, const unsigned lo
   return lo;
 }
 
-__global__ void k_level_hist(long long n, int base, unsigned long long seed, Thresholds th, int* counts) {
+// Level of a point in a batched build: the set's own thresholds
+// first * growth^k / n_set of the priority range.
+__device__ __forceinline__ int set_level(const DevTree& T, int vid, unsigned long long pr, const Thresholds& th) {
+  const double t0 = th.first / (double)T.sets[set_index(T, vid)].n * 4294967296.0;
+  if ((double)pr < t0) return 0;
+  const int k = 1 + (int)floor(log((double)pr / t0) / th.lgrow);
+  return k < th.n - 1 ? k : th.n - 1;
+}
+
+__global__ void k_level_hist(DevTree T, long long n, int base, unsigned long long seed, Thresholds th,
+                             int* counts) {
   __shared__ int sh[kMaxLevels];
   __shared__ unsigned long long st[kMaxLevels];
   for (int k = threadIdx.x; k < kMaxLevels; k += blockDim.x) {
@@ -223,7 +241,10 @@ __global__ void k_level_hist(long long n, int base, unsigned long long seed, Thr
   __syncthreads();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    atomicAdd(&sh[level_of(priority((uint32_t)(base + i), seed), st, th.n)], 1);
+  {
+    const unsigned long long pr = priority((uint32_t)(base + i), seed);
+    atomicAdd(&sh[T.nsets == 1 ? level_of(pr, st, th.n) : set_level(T, base + (int)i, pr, th)], 1);
+  }
   __syncthreads();
   for (int k = threadIdx.x; k < th.n; k += blockDim.x)
     if (sh[k]) atomicAdd(counts + k, sh[k]);
@@ -260,7 +281,8 @@ __global__ void k_level_order(DevTree T, long long n, int base, unsigned long lo
     const long long i = b + threadIdx.x;
     int lev = -1, rank = 0;
     if (i < n) {
-      lev = level_of(priority((uint32_t)(base + i), seed), st, th.n);
+      const unsigned long long pr = priority((uint32_t)(base + i), seed);
+      lev = T.nsets == 1 ? level_of(pr, st, th.n) : set_level(T, base + (int)i, pr, th);
       rank = atomicAdd(&cnt[lev], 1);
     }
     __syncthreads();
@@ -324,9 +346,10 @@ __global__ void k_activate(DevTree T, unsigned long long seed) {
       }
       pr = priority((uint32_t)vid, seed);
       const vdp::VPt p = load_pt(T, vid);
+      const SetGeo& g = T.sets[set_index(T, vid)];
       cur = -1;
-      for (int l = T.hint_levels; l >= 0 && cur < 0; --l) cur = T.hint[hint_index<D>(T, p, l)];
-      if (cur < 0) cur = 0;  // no insertion yet: the super simplex
+      for (int l = g.hint_levels; l >= 0 && cur < 0; --l) cur = T.hint[hint_index<D>(g, p, l)];
+      if (cur < 0) cur = g.root;  // no insertion into the set yet: its super simplex
       int4 v, nn;
       load_simplex(T, cur, v, nn);
       for (int k = 0; k < 64 && v.x < 0; ++k) {  // dead slot: follow it into its star
@@ -1071,7 +1094,7 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last) {
       write_star_big<D>(T, F, ID, nfac, round, P + kOffR, lane);
     }
     if (lane == 0) {
-      write_hints<D>(T, load_pt(T, cd.x), id0);
+      write_hints<D>(T, cd.x, load_pt(T, cd.x), id0);
       T.cinfo[c].w = ST_DONE;
       T.act[par][cd.w].x = -1;
     }
@@ -1246,23 +1269,23 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
 
 }  // namespace
 
-void launch_upload(const DevTree& T, const Launch& L, int dim, const double* d_xyz, int64_t n,
-                   int base_vid, const int* super_order) {
+void launch_upload(const DevTree& T, const Launch& L, int dim, const double* d_xyz, int64_t n, int base_vid) {
   note_launches(1);
-  int4 sup = make_int4(super_order[0], super_order[1], super_order[2], super_order[3]);
   if (dim == 3)
-    k_upload<3><<<L.blocks, 256, 0, L.stream>>>(T, d_xyz, n, base_vid, sup);
+    k_upload<3><<<L.blocks, 256, 0, L.stream>>>(T, d_xyz, n, base_vid);
   else
-    k_upload<2><<<L.blocks, 256, 0, L.stream>>>(T, d_xyz, n, base_vid, sup);
+    k_upload<2><<<L.blocks, 256, 0, L.stream>>>(T, d_xyz, n, base_vid);
 }
 
 void launch_levels(const DevTree& T, const Launch& L, int64_t n, int base_vid, uint64_t seed,
-                   const unsigned long long* thr, int nlev, int* d_work) {
+                   const unsigned long long* thr, int nlev, double first, double growth, int* d_work) {
   note_launches(3);
   Thresholds th;
   th.n = nlev;
+  th.first = first;
+  th.lgrow = log(growth);
   for (int k = 0; k < kMaxLevels; ++k) th.t[k] = k < nlev ? thr[k] : ~0ull;
-  k_level_hist<<<L.blocks, 256, 0, L.stream>>>(n, base_vid, seed, th, d_work);
+  k_level_hist<<<L.blocks, 256, 0, L.stream>>>(T, n, base_vid, seed, th, d_work);
   k_level_init<<<1, 32, 0, L.stream>>>(T, d_work, nlev);
   k_level_order<<<L.blocks, 256, 0, L.stream>>>(T, n, base_vid, seed, th, d_work + kMaxLevels);
 }

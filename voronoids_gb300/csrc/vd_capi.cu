@@ -145,9 +145,6 @@ struct vd_tree {
   int64_t cap_loc = 0;
   int64_t ncells = 0;
   // pinned staging for small host<->device copies
-  vdp::VPt h_sv[4];
-  vdp::FPt h_sf[4];
-  vd::Simplex h_s0;
   unsigned long long* h_mm = nullptr;
   // device staging of host input points (one-shot host path)
   double* d_in = nullptr;
@@ -179,6 +176,20 @@ struct vd_tree {
   };
   std::vector<ChunkGraph> graphs;
   bool use_graphs = true;
+  bool has_geometry = false;  // a super simplex exists (vd_tree_create leaves none)
+  // sets (one unless built by vd_batch_*): first input point of each set
+  int nsets = 1;
+  std::vector<long long> set_off;   // nsets + 1 (batched build)
+  int64_t cap_sets = 0;              // capacity of T.sets and the per-set scratch
+  long long* d_setoff = nullptr;     // nsets + 1
+  long long* d_eoff = nullptr;       // nsets + 1 edge offsets
+  double* d_cr = nullptr;            // 4 per set: sizing centre and radius
+  int* d_flags = nullptr;            // per set: some point not strictly inside
+  unsigned long long* d_mm = nullptr;  // 6 per set: bounding-box keys
+  int64_t cap_setof = 0;
+  // highest simplex slot handed out since the last reset: slots below it
+  // may hold simplices of an earlier build and are cleared on reset
+  int64_t simp_hwm = 0;
 };
 
 namespace {
@@ -242,7 +253,9 @@ struct ScopedProf {
 
 int sync_counters(vd_tree* t) {
   cudaMemcpyAsync(t->hctr, t->T.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, t->stream);
-  return cuda_status(cudaStreamSynchronize(t->stream));
+  const int rc = cuda_status(cudaStreamSynchronize(t->stream));
+  t->simp_hwm = std::max<int64_t>(t->simp_hwm, t->hctr->nsimp);
+  return rc;
 }
 
 // Grow a device array to `want` elements, keeping the first `keep` elements,
@@ -337,6 +350,13 @@ void drop_graphs(vd_tree* t) {
 
 void release(vd_tree* t) {
   drop_graphs(t);
+  dfree(t->T.sets);
+  dfree(t->T.set_of);
+  dfree(t->d_setoff);
+  dfree(t->d_eoff);
+  dfree(t->d_cr);
+  dfree(t->d_flags);
+  dfree(t->d_mm);
   if (!t) return;
   if (t->stream) cudaStreamSynchronize(t->stream);
   dfree(t->T.pts);
@@ -390,6 +410,33 @@ void release(vd_tree* t) {
 }
 
 // Device, stream and pools of an empty tree of dimension `dim`.
+// Finest location-hint level of a single-set tree (its size is not known
+// when it is created) and of a set of n points in a batched build (about two
+// points per finest cell).
+int single_hint_levels(int dim) { return dim == 3 ? 6 : 9; }
+int set_hint_levels(int dim, int64_t n) {
+  int l = 0;
+  const int per = dim == 3 ? 8 : 4;
+  for (int64_t cells = per; cells * 2 <= n && l < single_hint_levels(dim); cells *= per) ++l;
+  return l;
+}
+
+int ensure_sets(vd_tree* t, int64_t nsets) {
+  if (nsets <= t->cap_sets) return vd::E_OK;
+  const int64_t c = std::max<int64_t>(nsets, 2 * t->cap_sets);
+  dfree(t->T.sets);
+  dfree(t->d_setoff);
+  dfree(t->d_eoff);
+  dfree(t->d_cr);
+  dfree(t->d_flags);
+  dfree(t->d_mm);
+  if (dalloc(&t->T.sets, c) || dalloc(&t->d_setoff, c + 1) || dalloc(&t->d_eoff, c + 1) ||
+      dalloc(&t->d_cr, 4 * c) || dalloc(&t->d_flags, c) || dalloc(&t->d_mm, 6 * c))
+    return vd::E_NOMEM;
+  t->cap_sets = c;
+  return vd::E_OK;
+}
+
 int alloc_tree(vd_tree* t, int dim, void* stream) {
   t->dim = dim;
   t->ns = dim + 1;
@@ -418,10 +465,11 @@ int alloc_tree(vd_tree* t, int dim, void* stream) {
   if (cudaMallocHost((void**)&t->h_mm, 8 * sizeof(unsigned long long)) != cudaSuccess) return vd::E_NOMEM;
   t->T.cap_wchunk = t->sms * 20;
   if (dalloc(&t->T.wchunk, t->T.cap_wchunk)) return vd::E_NOMEM;
-  t->T.hint_levels = dim == 3 ? 6 : 9;
-  t->ncells = dim == 3 ? ((1LL << (3 * (t->T.hint_levels + 1))) - 1) / 7
-                       : ((1LL << (2 * (t->T.hint_levels + 1))) - 1) / 3;
+  t->ncells = vd::hint_cells(dim, single_hint_levels(dim));
   if (dalloc(&t->T.hint, t->ncells)) return vd::E_NOMEM;
+  if (ensure_sets(t, 1)) return vd::E_NOMEM;
+  t->T.nsets = 1;
+  t->T.nsuper = t->ns;
   t->cap_verts = t->ns + 16;
   if (dalloc(&t->T.pts, t->cap_verts) || dalloc(&t->T.ptf, t->cap_verts)) return vd::E_NOMEM;
   t->T.cap_verts = (int)t->cap_verts;
@@ -431,58 +479,125 @@ int alloc_tree(vd_tree* t, int dim, void* stream) {
   return vd::E_OK;
 }
 
-// (Re)starts the tree as the single super simplex for the bounding sphere
-// (centre c, radius rb) of the sizing points.  Pools keep their capacity.
-int set_geometry(vd_tree* t, const double* c, double rb) {
-  const int dim = t->dim;
-  ref_super_from_sphere(dim, c, rb, t->sup, &t->R);
-  if (!(t->R > 0.0) || !isfinite(t->R)) return vd::E_DEGENERATE;
-  for (int i = 0; i < t->ns; ++i)
+// Super simplex of one set for its bounding sphere (centre c, radius rb):
+// the reference's vertices and the vertex order that orients it positively.
+int set_super(int dim, const double* c, double rb, double sup[4][3], double* R, int order[4]) {
+  ref_super_from_sphere(dim, c, rb, sup, R);
+  if (!(*R > 0.0) || !isfinite(*R)) return vd::E_DEGENERATE;
+  for (int i = 0; i <= dim; ++i)
     for (int j = 0; j < 3; ++j)
-      if (!isfinite(t->sup[i][j]) || !coord_ok(t->sup[i][j])) return vd::E_RANGE;
-  t->sup_order[0] = 0;
-  t->sup_order[1] = 1;
-  t->sup_order[2] = 2;
-  t->sup_order[3] = dim == 3 ? 3 : -1;
-  {  // positive orientation of the super simplex
-    vdp::VPt v[4];
-    for (int i = 0; i < 4; ++i) v[i] = vdp::VPt{t->sup[i][0], t->sup[i][1], t->sup[i][2], 0.0};
-    vdp::Tally tl = {0, 0, 0, 0};
-    int err = 0;
-    int neg = dim == 3 ? vdp::exit_face<3, true>(v, v[3], 1u << 3, tl, err)
-                       : vdp::exit_face<2, true>(v, v[2], 1u << 2, tl, err);
-    if (neg >= 0) {
-      std::swap(t->sup_order[0], t->sup_order[1]);
-      vdp::VPt w[4] = {v[1], v[0], v[2], v[3]};
-      int neg2 = dim == 3 ? vdp::exit_face<3, true>(w, w[3], 1u << 3, tl, err)
-                          : vdp::exit_face<2, true>(w, w[2], 1u << 2, tl, err);
-      if (neg2 >= 0) return vd::E_DEGENERATE;
+      if (!isfinite(sup[i][j]) || !coord_ok(sup[i][j])) return vd::E_RANGE;
+  order[0] = 0;
+  order[1] = 1;
+  order[2] = 2;
+  order[3] = dim == 3 ? 3 : -1;
+  vdp::VPt v[4];
+  for (int i = 0; i < 4; ++i) v[i] = vdp::VPt{sup[i][0], sup[i][1], sup[i][2], 0.0};
+  vdp::Tally tl = {0, 0, 0, 0};
+  int err = 0;
+  const int neg = dim == 3 ? vdp::exit_face<3, true>(v, v[3], 1u << 3, tl, err)
+                           : vdp::exit_face<2, true>(v, v[2], 1u << 2, tl, err);
+  if (neg >= 0) {
+    std::swap(order[0], order[1]);
+    vdp::VPt w[4] = {v[1], v[0], v[2], v[3]};
+    const int neg2 = dim == 3 ? vdp::exit_face<3, true>(w, w[3], 1u << 3, tl, err)
+                              : vdp::exit_face<2, true>(w, w[2], 1u << 2, tl, err);
+    if (neg2 >= 0) return vd::E_DEGENERATE;
+  }
+  return vd::E_OK;
+}
+
+// (Re)starts the tree as `nsets` super simplices, one per set, for the
+// bounding spheres (centre c[3 s ..], radius rb[s]) of the sets' points;
+// `sizes` (batched build) gives the points of each set.  Pools keep their
+// capacity.
+int set_geometry_sets(vd_tree* t, int nsets, const double* c, const double* rb, const int64_t* sizes) {
+  const int dim = t->dim, nv = dim + 1;
+  if (nsets < 1 || (int64_t)nsets * nv > 0x40000000LL) return vd::E_ARG;
+  int rc = ensure_sets(t, nsets);
+  if (rc) return rc;
+  const int64_t ns = (int64_t)nsets * nv;
+  if (ns + 16 > t->cap_verts) {
+    int64_t cap = t->cap_verts, cap2 = t->cap_verts;
+    if (grow(&t->T.pts, &cap, ns + 16, 0, -1, t->stream)) return vd::E_NOMEM;
+    if (grow(&t->T.ptf, &cap2, ns + 16, 0, -1, t->stream)) return vd::E_NOMEM;
+    t->cap_verts = cap;
+    t->T.cap_verts = (int)cap;
+  }
+  rc = ensure_simplices(t, nsets + 1024);
+  if (rc) return rc;
+  std::vector<vdp::VPt> sv(ns);
+  std::vector<vdp::FPt> sf(ns);
+  std::vector<vd::Simplex> roots(nsets);
+  std::vector<vd::SetGeo> geo(nsets);
+  int64_t cells = 0;
+  for (int s = 0; s < nsets; ++s) {
+    double sup[4][3], R;
+    int order[4];
+    rc = set_super(dim, c + 3 * s, rb[s], sup, &R, order);
+    if (rc) return rc;
+    if (s == 0) {
+      memcpy(t->sup, sup, sizeof(sup));
+      t->R = R;
+      memcpy(t->sup_order, order, sizeof(order));
     }
+    for (int k = 0; k < nv; ++k) {
+      sv[(int64_t)s * nv + k] = vdp::VPt{sup[k][0], sup[k][1], sup[k][2], 0.0};
+      sf[(int64_t)s * nv + k] = vdp::split_point(sup[k][0], sup[k][1], sup[k][2]);
+    }
+    vd::SetGeo& g = geo[s];
+    for (int k = 0; k < 3; ++k) g.org[k] = (k < dim ? c[3 * s + k] : 0.0) - rb[s];
+    g.scale = rb[s] > 0 ? 1.0 / (2.0 * rb[s]) : 1.0;
+    g.hint_levels = sizes ? set_hint_levels(dim, sizes[s]) : single_hint_levels(dim);
+    g.hint_off = (int)cells;
+    g.root = s;
+    g.n = sizes ? (int)sizes[s] : 0;
+    for (int k = 0; k < 4; ++k) {
+      g.sup[k] = order[k] < 0 ? -1 : s * nv + order[k];
+      roots[s].v[k] = g.sup[k];
+      roots[s].n[k] = -1;
+    }
+    cells += vd::hint_cells(dim, g.hint_levels);
+    if (cells > 0x7fffffffLL) return vd::E_NOMEM;
   }
-  for (int k = 0; k < 3; ++k) t->T.gorg[k] = (k < dim ? c[k] : 0.0) - rb;
-  t->T.gscale = rb > 0 ? 1.0 / (2.0 * rb) : 1.0;
-  cudaMemsetAsync(t->T.hint, 0xff, sizeof(int) * t->ncells, t->stream);
+  if (cells > t->ncells) {
+    dfree(t->T.hint);
+    t->ncells = 0;
+    if (dalloc(&t->T.hint, cells)) return vd::E_NOMEM;
+    t->ncells = cells;
+  }
+  t->has_geometry = true;
+  t->nsets = nsets;
+  t->ns = (int)ns;
+  t->T.nsets = nsets;
+  t->T.nsuper = (int)ns;
+  cudaMemsetAsync(t->T.hint, 0xff, sizeof(int) * cells, t->stream);
   cudaMemsetAsync(t->T.wchunk, 0, sizeof(int2) * t->T.cap_wchunk, t->stream);
-  for (int i = 0; i < t->ns; ++i) {
-    t->h_sv[i] = vdp::VPt{t->sup[i][0], t->sup[i][1], t->sup[i][2], 0.0};
-    t->h_sf[i] = vdp::split_point(t->sup[i][0], t->sup[i][1], t->sup[i][2]);
-  }
-  cudaMemcpyAsync(t->T.pts, t->h_sv, sizeof(vdp::VPt) * t->ns, cudaMemcpyHostToDevice, t->stream);
-  cudaMemcpyAsync(t->T.ptf, t->h_sf, sizeof(vdp::FPt) * t->ns, cudaMemcpyHostToDevice, t->stream);
-  t->nverts = t->ns;
+  cudaMemcpyAsync(t->T.sets, geo.data(), sizeof(vd::SetGeo) * nsets, cudaMemcpyHostToDevice, t->stream);
+  cudaMemcpyAsync(t->T.pts, sv.data(), sizeof(vdp::VPt) * ns, cudaMemcpyHostToDevice, t->stream);
+  cudaMemcpyAsync(t->T.ptf, sf.data(), sizeof(vdp::FPt) * ns, cudaMemcpyHostToDevice, t->stream);
+  // Slots of an earlier build read as dead: a warp that takes a new chunk
+  // of fresh slots leaves the rest of its old chunk unwritten, and such
+  // slots must not show an old simplex.
+  const int64_t used = std::min<int64_t>(std::max<int64_t>(t->simp_hwm, t->hctr->nsimp), t->T.cap_simp);
+  if (used > 0) cudaMemsetAsync(t->T.simp, 0xff, sizeof(vd::Simplex) * used, t->stream);
+  t->simp_hwm = nsets;
+  cudaMemcpyAsync(t->T.simp, roots.data(), sizeof(vd::Simplex) * nsets, cudaMemcpyHostToDevice, t->stream);
+  t->nverts = ns;
   t->inserted = 0;
   t->round_base = t->round;
   t->edges_valid = false;
-  for (int i = 0; i < 4; ++i) {
-    t->h_s0.v[i] = t->sup_order[i];
-    t->h_s0.n[i] = -1;
-  }
-  cudaMemcpyAsync(t->T.simp, &t->h_s0, sizeof(vd::Simplex), cudaMemcpyHostToDevice, t->stream);
   memset(t->hctr, 0, sizeof(Counters));
-  t->hctr->nsimp = 1;
+  t->hctr->nsimp = nsets;
   t->hctr->round = t->round - 1;  // the next k_plan opens round t->round
   cudaMemcpyAsync(t->T.ctr, t->hctr, sizeof(Counters), cudaMemcpyHostToDevice, t->stream);
   return cuda_status(cudaStreamSynchronize(t->stream));
+}
+
+// Single-set tree: the reference's DelaunayTree.
+int set_geometry(vd_tree* t, const double* c, double rb) {
+  t->set_off.clear();
+  return set_geometry_sets(t, 1, c, &rb, nullptr);
 }
 
 int check_host_points(int dim, const double* pts, int64_t n) {
@@ -709,7 +824,7 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
 // early rounds, which can only insert a few points into a small
 // triangulation, do not locate, relocate or nominate the whole input.
 int insert_device(vd_tree* t, const double* d_xyz, int64_t n, uint64_t seed) {
-  if (n < 0 || (n > 0 && !d_xyz)) return vd::E_ARG;
+  if (n < 0 || (n > 0 && !d_xyz) || !t->has_geometry) return vd::E_ARG;
   if (n == 0) return vd::E_OK;
   int rc = ensure_points(t, n);
   if (rc) return rc;
@@ -719,10 +834,13 @@ int insert_device(vd_tree* t, const double* d_xyz, int64_t n, uint64_t seed) {
   t->edges_valid = false;
   const vd::Launch L = launch_of(t);
   const int base = (int)t->nverts;
-  vd::launch_upload(t->T, L, t->dim, d_xyz, n, base, t->sup_order);
+  vd::launch_upload(t->T, L, t->dim, d_xyz, n, base);
+  // priority levels: thresholds of the one set, or a level count covering
+  // the largest set of a batched build (each set computes its own)
   std::vector<unsigned long long> thr;
-  {
-    double m = std::min<double>((double)std::max<int64_t>(t->first_prefix, 1), (double)n);
+  const double first = (double)std::max<int64_t>(t->first_prefix, 1);
+  if (t->nsets == 1) {
+    double m = std::min<double>(first, (double)n);
     while ((int)thr.size() < vd::kMaxLevels - 1) {
       const double f = m / (double)n;
       if (f >= 1.0) break;
@@ -730,9 +848,15 @@ int insert_device(vd_tree* t, const double* d_xyz, int64_t n, uint64_t seed) {
       m = std::max(m * t->growth, m + 1.0);
     }
     thr.push_back(1ull << 32);
+  } else {
+    long long big = 1;
+    for (int s = 0; s < t->nsets; ++s) big = std::max(big, t->set_off[s + 1] - t->set_off[s]);
+    int nlev = 1;
+    for (double m = first; m < (double)big && nlev < vd::kMaxLevels; m *= t->growth) ++nlev;
+    thr.assign(nlev, 1ull << 32);
   }
   cudaMemsetAsync(t->d_counts, 0, sizeof(int) * 2 * vd::kMaxLevels, t->stream);
-  vd::launch_levels(t->T, L, n, base, seed, thr.data(), (int)thr.size(), t->d_counts);
+  vd::launch_levels(t->T, L, n, base, seed, thr.data(), (int)thr.size(), first, t->growth, t->d_counts);
   rc = sync_counters(t);
   if (rc) return rc;
   if (t->hctr->err) return t->hctr->err;
@@ -818,6 +942,98 @@ int compute_edges(vd_tree* t, uint2* out = nullptr, int64_t cap = 0, int64_t* m 
     t->edges_valid = true;
   }
   return vd::E_OK;
+}
+
+// Bounding sphere (centre, radius before the reference's 1.5 growth) from
+// the order-preserving bounding-box keys of k_bbox / k_set_bbox; the same
+// arithmetic as src/geometry.rs:99-131.
+int sphere_from_keys(int dim, const unsigned long long* mm, double* c, double* r0) {
+  auto dec = [](unsigned long long key) {
+    const unsigned long long b = (key >> 63) ? (key & 0x7fffffffffffffffull) : ~key;
+    double x;
+    memcpy(&x, &b, 8);
+    return x;
+  };
+  double lo[3], hi[3];
+  for (int k = 0; k < dim; ++k) {
+    lo[k] = dec(mm[k]);
+    hi[k] = dec(mm[3 + k]);
+    if (!isfinite(lo[k]) || !isfinite(hi[k])) return vd::E_NONFINITE;
+    c[k] = (hi[k] + lo[k]) / 2.0;
+  }
+  for (int k = dim; k < 3; ++k) c[k] = 0.0;
+  double su = 0.0, sl = 0.0;
+  for (int i = 0; i < dim; ++i) su += (hi[i] - c[i]) * (hi[i] - c[i]);
+  for (int i = 0; i < dim; ++i) sl += (lo[i] - c[i]) * (lo[i] - c[i]);
+  const double ud = sqrt(su), ld = sqrt(sl);
+  *r0 = ud > ld ? ud : ld;
+  return vd::E_OK;
+}
+
+// Batched build: sizes every set's super simplex from its points (device
+// reductions, one block per set), then restarts the tree with one super
+// simplex per set.
+int batch_reset_device(vd_tree* t, const double* d_pts, const int64_t* offsets, int nsets) {
+  if (!d_pts || !offsets || nsets < 1 || offsets[0] != 0) return vd::E_ARG;
+  for (int s = 0; s < nsets; ++s)
+    if (offsets[s + 1] <= offsets[s]) return vd::E_ARG;  // every set needs a point
+  const int64_t n = offsets[nsets];
+  if (n + (int64_t)nsets * (t->dim + 1) > 0x7ffffff0LL) return vd::E_ARG;
+  int rc = ensure_sets(t, nsets);
+  if (rc) return rc;
+  const vd::Launch L = launch_of(t);
+  t->set_off.assign(offsets, offsets + nsets + 1);
+  cudaMemcpyAsync(t->d_setoff, t->set_off.data(), sizeof(long long) * (nsets + 1), cudaMemcpyHostToDevice,
+                  t->stream);
+  std::vector<unsigned long long> mm(6 * (size_t)nsets);
+  vd::launch_set_bbox(L, t->dim, d_pts, t->d_setoff, nsets, t->d_mm);
+  cudaMemcpyAsync(mm.data(), t->d_mm, sizeof(unsigned long long) * mm.size(), cudaMemcpyDeviceToHost, t->stream);
+  if (cudaStreamSynchronize(t->stream) != cudaSuccess) return vd::E_CUDA;
+  std::vector<double> c(3 * (size_t)nsets), cr(4 * (size_t)nsets), rb(nsets);
+  std::vector<int64_t> sizes(nsets);
+  for (int s = 0; s < nsets; ++s) {
+    rc = sphere_from_keys(t->dim, &mm[6 * (size_t)s], &c[3 * (size_t)s], &rb[s]);
+    if (rc) return rc;
+    for (int k = 0; k < 3; ++k) cr[4 * (size_t)s + k] = c[3 * (size_t)s + k];
+    cr[4 * (size_t)s + 3] = rb[s];
+    sizes[s] = offsets[s + 1] - offsets[s];
+  }
+  std::vector<int> flags(nsets);
+  cudaMemcpyAsync(t->d_cr, cr.data(), sizeof(double) * cr.size(), cudaMemcpyHostToDevice, t->stream);
+  vd::launch_set_outside(L, t->dim, d_pts, t->d_setoff, nsets, t->d_cr, t->d_flags);
+  cudaMemcpyAsync(flags.data(), t->d_flags, sizeof(int) * nsets, cudaMemcpyDeviceToHost, t->stream);
+  if (cudaStreamSynchronize(t->stream) != cudaSuccess) return vd::E_CUDA;
+  for (int s = 0; s < nsets; ++s)
+    if (flags[s]) rb[s] *= 1.5;
+  rc = set_geometry_sets(t, nsets, c.data(), rb.data(), sizes.data());
+  if (rc) return rc;
+  t->set_off.assign(offsets, offsets + nsets + 1);
+  if (n > t->cap_setof) {
+    dfree(t->T.set_of);
+    t->cap_setof = 0;
+    if (dalloc(&t->T.set_of, n)) return vd::E_NOMEM;
+    t->cap_setof = n;
+  }
+  vd::launch_set_fill(L, t->d_setoff, nsets, t->T.set_of);
+  return vd::E_OK;
+}
+
+// Edges of a batched build into d_uv (numbers within each set) and the
+// host edge offsets of the sets.
+int batch_edges(vd_tree* t, uint2* d_uv, int64_t cap, int64_t* edge_offsets, int64_t* n_edges) {
+  int64_t m = 0;
+  int rc = compute_edges(t, d_uv, cap, &m);
+  if (n_edges) *n_edges = m;
+  if (rc) return rc;
+  const vd::Launch L = launch_of(t);
+  vd::launch_set_edge_offsets(L, t->es.uoff, t->d_setoff, t->nsets, t->d_eoff);
+  cudaMemcpyAsync(edge_offsets, t->d_eoff, sizeof(long long) * (t->nsets + 1), cudaMemcpyDeviceToHost, t->stream);
+  if (m > cap) {
+    if (cudaStreamSynchronize(t->stream) != cudaSuccess) return vd::E_CUDA;
+    return vd::E_ARG;
+  }
+  vd::launch_localize(L, d_uv, m, t->T.set_of, t->d_setoff);
+  return cuda_status(cudaStreamSynchronize(t->stream));
 }
 
 }  // namespace
@@ -941,14 +1157,14 @@ void vd_tree_free(vd_tree* t) {
 static int ready(vd_tree* t) { return (t && t->hctr && t->T.ctr) ? VD_OK : VD_ERR_ARG; }
 
 int vd_insert_points_device(vd_tree* t, const double* d_pts, int64_t n, uint64_t seed) {
-  if (ready(t)) return VD_ERR_ARG;
+  if (ready(t) || t->nsets != 1) return VD_ERR_ARG;  // batched trees take no further points
   int rc = insert_device(t, d_pts, n, seed);
   if (rc == VD_OK && t->hctr->ndup > 0) rc = VD_ERR_DUPLICATE;
   return rc;
 }
 
 int vd_insert_points(vd_tree* t, const double* pts, int64_t n, uint64_t seed) {
-  if (ready(t)) return VD_ERR_ARG;
+  if (ready(t) || t->nsets != 1) return VD_ERR_ARG;  // batched trees take no further points
   int rc = insert_host(t, pts, n, seed);
   if (rc == VD_OK && t->hctr->ndup > 0) rc = VD_ERR_DUPLICATE;
   return rc;
@@ -1064,7 +1280,8 @@ int vd_check_delaunay(vd_tree* t, int* ok, int64_t* violations) {
   if (rc) return rc;
   if (violations)
     for (int k = 0; k < 6; ++k) violations[k] = (int64_t)h[k];
-  *ok = (h[0] == 0 && h[1] == 0 && h[2] == 0 && h[3] == 0 && h[4] == (unsigned long long)(t->dim + 1)) ? 1 : 0;
+  const unsigned long long hull = (unsigned long long)t->nsets * (t->dim + 1);  // the super simplices' faces
+  *ok = (h[0] == 0 && h[1] == 0 && h[2] == 0 && h[3] == 0 && h[4] == hull) ? 1 : 0;
   return t->hctr->err ? t->hctr->err : VD_OK;
 }
 
@@ -1203,6 +1420,70 @@ int vd_trace(vd_tree* t, int64_t* rows, int64_t cap, int64_t* n) {
   if (!rows) return VD_OK;
   if (cap < *n) return VD_ERR_ARG;
   std::copy(t->trace_rows.begin(), t->trace_rows.end(), rows);
+  return VD_OK;
+}
+
+vd_tree* vd_tree_create(int dim, void* stream, int* status) {
+  vd_tree* t = new (std::nothrow) vd_tree();
+  if (!t) {
+    if (status) *status = VD_ERR_NOMEM;
+    return nullptr;
+  }
+  const int rc = (dim == 2 || dim == 3) ? alloc_tree(t, dim, stream) : VD_ERR_ARG;
+  if (status) *status = rc;
+  return t;
+}
+
+int vd_batch_delaunay_device(vd_tree* t, const double* d_pts, const int64_t* offsets, int nsets, uint64_t seed,
+                             uint32_t* d_uv, int64_t cap, int64_t* edge_offsets) {
+  if (ready(t) || !edge_offsets || (!d_uv && cap > 0)) return VD_ERR_ARG;
+  int rc = batch_reset_device(t, d_pts, offsets, nsets);
+  if (rc) return rc;
+  rc = insert_device(t, d_pts, offsets[nsets], seed);
+  if (rc == VD_OK && t->hctr->ndup > 0) rc = VD_ERR_DUPLICATE;
+  if (rc && rc != VD_ERR_DUPLICATE) return rc;
+  const int rc2 = batch_edges(t, reinterpret_cast<uint2*>(d_uv), cap, edge_offsets, nullptr);
+  return rc2 ? rc2 : rc;
+}
+
+int vd_batch_delaunay(vd_tree* t, const double* pts, const int64_t* offsets, int nsets, uint64_t seed,
+                      uint32_t* uv, int64_t cap, int64_t* edge_offsets) {
+  if (ready(t) || !pts || !offsets || nsets < 1 || !edge_offsets || (!uv && cap > 0)) return VD_ERR_ARG;
+  const int64_t n = offsets[nsets];
+  if (n < 1) return VD_ERR_ARG;
+  int rc = check_host_points(t->dim, pts, n);
+  if (rc) return rc;
+  if (n * t->dim > t->cap_in) {
+    dfree(t->d_in);
+    t->cap_in = 0;
+    if (dalloc(&t->d_in, (size_t)(n * t->dim))) return VD_ERR_NOMEM;
+    t->cap_in = n * t->dim;
+  }
+  cudaMemcpyAsync(t->d_in, pts, sizeof(double) * n * t->dim, cudaMemcpyHostToDevice, t->stream);
+  rc = batch_reset_device(t, t->d_in, offsets, nsets);
+  if (rc) return rc;
+  rc = insert_device(t, t->d_in, n, seed);
+  if (rc == VD_OK && t->hctr->ndup > 0) rc = VD_ERR_DUPLICATE;
+  if (rc && rc != VD_ERR_DUPLICATE) return rc;
+  // edges into the tree's own buffer, numbered within their sets, then out
+  int64_t m = 0;
+  int rc2 = sync_counters(t);
+  if (!rc2) rc2 = ensure_edge_scratch(t, t->nverts - t->ns, t->hctr->nsimp);
+  if (!rc2) {
+    t->edges_valid = false;  // the buffer holds set-local numbers
+    rc2 = batch_edges(t, t->d_edges, t->cap_edges, edge_offsets, &m);
+  }
+  if (!rc2 && uv) {
+    if (cap < m) return VD_ERR_ARG;
+    cudaMemcpyAsync(uv, t->d_edges, sizeof(uint2) * m, cudaMemcpyDeviceToHost, t->stream);
+    rc2 = cuda_status(cudaStreamSynchronize(t->stream));
+  }
+  return rc2 ? rc2 : rc;
+}
+
+int vd_num_sets(vd_tree* t, int* nsets) {
+  if (ready(t) || !nsets) return VD_ERR_ARG;
+  *nsets = t->nsets;
   return VD_OK;
 }
 

@@ -98,6 +98,26 @@ struct Counters {
 // geometrically growing size; at most this many.
 constexpr int kMaxLevels = 96;
 
+// One point set of a tree.  A tree holds a single set (the reference's
+// DelaunayTree) or many independent sets triangulated together (batched
+// build).  Vertex ids: the super-simplex vertices of all sets come first,
+// D + 1 per set, then the input points of all sets in input order; set s
+// starts with simplex slot s, its super simplex.
+struct alignas(16) SetGeo {
+  double org[3];    // location-hint grid origin (centre - bounding radius)
+  double scale;     // 1 / grid extent
+  int hint_off;     // first hint cell of the set
+  int hint_levels;  // finest hint level (2^l cells per axis)
+  int root;         // slot of the set's super simplex
+  int n;            // input points of the set (batched build)
+  int sup[4];       // super-simplex vertex ids, positively oriented (-1 pads 2D)
+};
+
+// Hint cells of levels 0..levels.
+__host__ __device__ inline long long hint_cells(int dim, int levels) {
+  return dim == 3 ? ((1LL << (3 * (levels + 1))) - 1) / 7 : ((1LL << (2 * (levels + 1))) - 1) / 3;
+}
+
 struct DevTree {
   vdp::VPt* pts;
   vdp::FPt* ptf;      // the same coordinates split into f32 hi/lo pairs
@@ -119,10 +139,11 @@ struct DevTree {
   int cap_wchunk;
   int* order;         // vertex ids of the current call grouped by priority level
   int* lev_off;       // kMaxLevels + 1 offsets of the levels in `order`
-  int* hint;          // location hints, levels 0..hint_levels (see vd_build.cu)
-  int hint_levels;
-  double gorg[3];     // hint grid origin and 1 / extent
-  double gscale;
+  int* hint;          // location hints of all sets (see vd_build.cu)
+  SetGeo* sets;       // nsets entries
+  int* set_of;        // set of input point (vid - nsuper); unused when nsets == 1
+  int nsets;
+  int nsuper;         // vertex ids below this are super-simplex vertices
   int cap_simp;
   int cap_verts;
   int cap_pool;
@@ -161,6 +182,9 @@ __device__ inline void set_error(Counters* c, int code) { atomicCAS(&c->err, 0, 
 // into an out-of-bounds access.
 __device__ inline bool bad_simp(const DevTree& T, int s) { return (unsigned)s >= (unsigned)T.cap_simp; }
 __device__ inline bool bad_vert(const DevTree& T, int v) { return (unsigned)v >= (unsigned)T.cap_verts; }
+__device__ inline int set_index(const DevTree& T, int vid) {
+  return T.nsets == 1 ? 0 : T.set_of[vid - T.nsuper];
+}
 #endif
 
 // Kernels launched by this library in this process (diagnostics).
@@ -174,15 +198,17 @@ struct Launch {
   cudaStream_t stream;
 };
 
-void launch_upload(const DevTree& T, const Launch& L, int dim, const double* d_xyz, int64_t n,
-                   int base_vid, const int* super_order);
-// Priority levels of the points base_vid .. base_vid + n - 1: level k holds
-// the priorities in [thr[k-1], thr[k]).  d_work holds 2 * kMaxLevels ints
-// (counts, cursors) and must be zero on entry; on exit T.order lists the
-// points level by level, T.lev_off[0..nlev] bounds the levels and the feed
-// counters are reset to level 0.
+// Writes the points (and their split f32 form) as vertices base_vid.. and
+// checks that each lies strictly inside its set's super simplex.
+void launch_upload(const DevTree& T, const Launch& L, int dim, const double* d_xyz, int64_t n, int base_vid);
+// Priority levels of the points base_vid .. base_vid + n - 1.  With one set,
+// level k holds the priorities in [thr[k-1], thr[k]); with many, each set
+// has its own levels, of `first` points growing by `growth`, sized by the
+// set.  d_work holds 2 * kMaxLevels ints (counts, cursors) and must be zero
+// on entry; on exit T.order lists the points level by level,
+// T.lev_off[0..nlev] bounds the levels and the feed counters are reset.
 void launch_levels(const DevTree& T, const Launch& L, int64_t n, int base_vid, uint64_t seed,
-                   const unsigned long long* thr, int nlev, int* d_work);
+                   const unsigned long long* thr, int nlev, double first, double growth, int* d_work);
 // Feed of one round: activate priority levels while the active points are
 // fewer than `ratio` times the inserted ones (at least one level when none
 // is active).
@@ -236,6 +262,22 @@ void launch_bbox(const Launch& L, int dim, const double* d_xyz, int64_t n, unsig
 void launch_outside(const Launch& L, int dim, const double* d_xyz, int64_t n, const double* c, double r0,
                     int* d_flag);
 void launch_close_chunks(const DevTree& T, const Launch& L);
+// Batched build (vd_size.cu).  off[0..nsets] are the sets' first points
+// (int64, device).  Per-set bounding box as order-preserving keys (mm[6 s +
+// 0..2] minima, +3..5 maxima), the reference's "point not strictly inside"
+// test against (cr[4 s + 0..2] centre, cr[4 s + 3] radius), and the set of
+// every point.
+void launch_set_bbox(const Launch& L, int dim, const double* d_xyz, const long long* off, int nsets,
+                     unsigned long long* d_mm);
+void launch_set_outside(const Launch& L, int dim, const double* d_xyz, const long long* off, int nsets,
+                        const double* cr, int* d_flags);
+void launch_set_fill(const Launch& L, const long long* off, int nsets, int* set_of);
+// Edge pairs of global point numbers -> numbers within their set.
+void launch_localize(const Launch& L, uint2* uv, int64_t m, const int* set_of, const long long* off);
+// Edge offsets of the sets: eoff[s] = uoff[off[s]] (uoff: per-point edge
+// offsets of the last extraction).
+void launch_set_edge_offsets(const Launch& L, const int* uoff, const long long* off, int nsets,
+                             long long* eoff);
 
 // Validator: out[0..5] = non-positive, asymmetric, not Delaunay (exact),
 // not perturbed-Delaunay, hull facets, facets checked.

@@ -95,7 +95,8 @@ void exclusive_scan(const int* in, int* out, long long n, int* tmp, cudaStream_t
 // ---- edge instances ---------------------------------------------------------
 template <int D>
 __global__ void k_edge_count(DevTree T, int nsimp, int n_in, int* cnt) {
-  constexpr int NV = D + 1, NS = D + 1;
+  constexpr int NV = D + 1;
+  const int NS = T.nsuper;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsimp; s += gridDim.x * blockDim.x) {
     const int4 v = reinterpret_cast<const int4*>(T.simp + s)[0];
     if (v.x < 0) continue;
@@ -115,7 +116,8 @@ __global__ void k_edge_count(DevTree T, int nsimp, int n_in, int* cnt) {
 
 template <int D>
 __global__ void k_edge_fill(DevTree T, int nsimp, int n_in, int* cnt, const int* off, int* buf) {
-  constexpr int NV = D + 1, NS = D + 1;
+  constexpr int NV = D + 1;
+  const int NS = T.nsuper;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsimp; s += gridDim.x * blockDim.x) {
     const int4 v = reinterpret_cast<const int4*>(T.simp + s)[0];
     if (v.x < 0) continue;

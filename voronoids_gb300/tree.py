@@ -74,6 +74,65 @@ class DelaunayTree:
             self._h = None
             raise VDError(st.value, "vd_tree_new")
 
+    @classmethod
+    def create(cls, dim, stream=None):
+        """An empty tree (no super simplex yet), e.g. for :meth:`batch`."""
+        L = _native.load()
+        st = ctypes.c_int(0)
+        h = L.vd_tree_create(int(dim), ctypes.c_void_p(stream) if stream is not None else None, ctypes.byref(st))
+        if not h:
+            raise VDError(3, "vd_tree_create")
+        self = cls.__new__(cls)
+        self.dim = int(dim)
+        self._h = ctypes.c_void_p(h)
+        if st.value != _native.VD_OK:
+            L.vd_tree_free(self._h)
+            self._h = None
+            raise VDError(st.value, "vd_tree_create")
+        return self
+
+    # -- batched build ------------------------------------------------------------
+    def batch(self, points, offsets, seed=0):
+        """Triangulate the sets ``points[offsets[s]:offsets[s+1]]`` together.
+
+        Returns ``(uv, edge_offsets)``: uint32 pairs numbered within each set
+        and the (nsets + 1) bounds of each set's edges."""
+        p = _points(points, self.dim)
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        nsets = off.shape[0] - 1
+        eoff = np.zeros(nsets + 1, dtype=np.int64)
+        L = _native.load()
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        cap = (10 if self.dim == 3 else 4) * p.shape[0] + 64  # above any uniform-density edge count
+        for _ in range(2):
+            uv = np.zeros((cap, 2), dtype=np.uint32)
+            rc = L.vd_batch_delaunay(self._h, _dp(p), off.ctypes.data_as(i64p), nsets, seed,
+                                     uv.ctypes.data_as(ctypes.c_void_p), cap, eoff.ctypes.data_as(i64p))
+            if rc == 1 and eoff[-1] > cap:  # more edges than the first guess: exact size
+                cap = int(eoff[-1])
+                continue
+            break
+        if rc not in (_native.VD_OK, _native.VD_ERR_DUPLICATE):
+            _check(rc, "batch")
+        return uv[: int(eoff[-1])], eoff
+
+    def batch_device(self, ptr, offsets, seed, out_ptr, cap):
+        """Device variant of :meth:`batch`; returns the edge offsets."""
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        nsets = off.shape[0] - 1
+        eoff = np.zeros(nsets + 1, dtype=np.int64)
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        rc = _native.load().vd_batch_delaunay_device(self._h, ctypes.c_void_p(ptr), off.ctypes.data_as(i64p), nsets,
+                                                     seed, ctypes.c_void_p(out_ptr), cap, eoff.ctypes.data_as(i64p))
+        if rc not in (_native.VD_OK, _native.VD_ERR_DUPLICATE):
+            _check(rc, "batch_device")
+        return eoff
+
+    def num_sets(self):
+        n = ctypes.c_int(0)
+        _check(_native.load().vd_num_sets(self._h, ctypes.byref(n)), "num_sets")
+        return n.value
+
     # -- lifetime ---------------------------------------------------------------
     def close(self):
         if getattr(self, "_h", None):
@@ -85,6 +144,12 @@ class DelaunayTree:
             self.close()
         except Exception:
             pass
+
+    def reset(self, points):
+        """Empty the tree and size its super simplex from ``points`` (host),
+        keeping its device allocations."""
+        p = _points(points, self.dim)
+        _check(_native.load().vd_tree_reset(self._h, _dp(p), p.shape[0]), "reset")
 
     # -- insertion --------------------------------------------------------------
     def add_points_to_tree(self, points, seed=0):
@@ -225,3 +290,21 @@ def delaunay(points, seed=0):
     t = DelaunayTree(p)
     t.add_points_to_tree(p, seed=seed)
     return t
+
+
+def delaunay_batch(point_sets, seed=0, tree=None):
+    """Triangulate many independent point sets in one batched build.
+
+    Returns one sorted (m, 2) int64 edge array per set, numbered within the
+    set; each equals ``delaunay(points, seed).edges()`` of that set alone."""
+    sets = [_points(p) for p in point_sets]
+    dim = sets[0].shape[1]
+    off = np.zeros(len(sets) + 1, dtype=np.int64)
+    off[1:] = np.cumsum([p.shape[0] for p in sets])
+    t = tree if tree is not None else DelaunayTree.create(dim)
+    try:
+        uv, eoff = t.batch(np.concatenate(sets, axis=0), off, seed=seed)
+    finally:
+        if tree is None:
+            t.close()
+    return [uv[eoff[s]:eoff[s + 1]].astype(np.int64) for s in range(len(sets))]
