@@ -33,6 +33,8 @@
 // which k_cavity detects and drops.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "vd_common.cuh"
 
 namespace vd {
@@ -776,7 +778,6 @@ struct WarpCommit {
   static constexpr int HR = D == 3 ? 512 : 256;  // ridge table slots (> 2x ridges)
   unsigned long long rk[HR];   // ridge key (r0 << 32 | r1)
   int ra[HR], rb[HR];          // the two half-ridges (facet << 2 | face)
-  int fr[6 * Cap<D>::MAXF];
   int id[Cap<D>::MAXF];
   int first[Cap<D>::MAXC];     // first facet index of each cavity simplex
   int freeslot[Cap<D>::MAXC];  // cavity slots without an own facet
@@ -816,7 +817,8 @@ __device__ __forceinline__ void emit_simplex(const DevTree& T, const int* r, int
 // into a shared-memory table keyed by the ridge's vertices; each ridge has
 // exactly two halves, which are each other's neighbours.
 template <int D>
-__device__ void write_star(const DevTree& T, WarpCommit<D>& W, int nfac, int qv, int round, int lane) {
+__device__ void write_star(const DevTree& T, WarpCommit<D>& W, const int* __restrict__ FR, int nfac, int qv,
+                           int round, int lane) {
   constexpr int NV = D + 1, HR = WarpCommit<D>::HR;
   const unsigned long long EMPTY = ~0ull;
   for (int i = lane; i < HR; i += 32) {
@@ -826,7 +828,7 @@ __device__ void write_star(const DevTree& T, WarpCommit<D>& W, int nfac, int qv,
   __syncwarp();
   for (int it = lane; it < nfac * NV; it += 32) {
     const int j = it / NV, g = it - j * NV;
-    const int* r = W.fr + 6 * j;
+    const int* r = FR + 6 * j;
     const int qf = r[5] & 3;
     if (g == qf) continue;
     int r0, r1;
@@ -843,7 +845,7 @@ __device__ void write_star(const DevTree& T, WarpCommit<D>& W, int nfac, int qv,
   }
   __syncwarp();
   for (int j = lane; j < nfac; j += 32) {
-    const int* r = W.fr + 6 * j;
+    const int* r = FR + 6 * j;
     const int qf = r[5] & 3;
     int4 nn = make_int4(-1, -1, -1, -1);
     nn = set4(nn, qf, r[4]);
@@ -865,7 +867,7 @@ __device__ void write_star(const DevTree& T, WarpCommit<D>& W, int nfac, int qv,
       const int m = other >> 2;
       int pos = -1;
       if (other >= 0 && m < nfac) {
-        const int* w = W.fr + 6 * m;
+        const int* w = FR + 6 * m;
         const int qm = w[5] & 3;
         for (int i = 0; i < NV; ++i)
           if (i != qm && w[i] != r0 && w[i] != r1) pos = i;
@@ -1045,9 +1047,8 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last) {
       // slot assignment: first facet of cavity simplex k takes k's slot;
       // the other facets take the remaining cavity slots, then fresh ones
       for (int i = lane; i < ncav; i += 32) W.first[i] = 0x7fffffff;
-      for (int x = lane; x < 6 * nfac; x += 32) W.fr[x] = F[x];
       __syncwarp();
-      for (int j = lane; j < nfac; j += 32) atomicMin(&W.first[W.fr[6 * j + 5] >> 2], j);
+      for (int j = lane; j < nfac; j += 32) atomicMin(&W.first[__ldg(F + 6 * j + 5) >> 2], j);
       __syncwarp();
       int nfree = 0;  // cavity slots without an own facet, ranked
       for (int i0 = 0; i0 < ncav; i0 += 32) {
@@ -1063,7 +1064,7 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last) {
         int id = 0;
         bool sec = false;
         if (j < nfac) {
-          const int k = W.fr[6 * j + 5] >> 2;
+          const int k = __ldg(F + 6 * j + 5) >> 2;
           sec = W.first[k] != j;
           if (!sec) id = P[k];
         }
@@ -1080,7 +1081,7 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last) {
       // leftover cavity slots become holes pointing into the star
       for (int t = nsec + lane; t < nfree; t += 32)
         store_simplex(T, W.freeslot[t], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
-      write_star<D>(T, W, nfac, cd.x, round, lane);
+      write_star<D>(T, W, F, nfac, cd.x, round, lane);
     } else {
       // large star (spilled search): plain slot assignment, ids in the
       // stretch's vertex-list area (free after the search), ridge table in
@@ -1236,6 +1237,9 @@ __global__ void k_relocate(DevTree T) {
   flush_tally(T.ctr, tl, 0, walk);
 }
 
+// Resident blocks of k_check<2>, k_check<3> on the whole GPU.
+int g_check_wave[2] = {1 << 20, 1 << 20};
+
 template <int D>
 void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed& fd, Prof* pf) {
   auto mark = [&](int type) {
@@ -1260,7 +1264,8 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
       k_reclaim<D><<<L.warps / 4, 128, 0, L.stream>>>(T, p);
       mark(KT_RECLAIM);
     }
-    k_check<D><<<L.warps / 4, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, p == tu.passes - 1);
+    k_check<D><<<std::min(L.warps / 4, g_check_wave[D - 2]), 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(
+        T, p, p == tu.passes - 1);
     mark(KT_CHECK);
   }
   k_relocate<D><<<L.blocks, 256, 0, L.stream>>>(T);
@@ -1295,7 +1300,17 @@ int prepare_round_kernels() {
                                               4 * (int)sizeof(WarpCommit<3>));
   const cudaError_t e2 = cudaFuncSetAttribute(k_check<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               4 * (int)sizeof(WarpCommit<2>));
-  return e3 == cudaSuccess && e2 == cudaSuccess ? E_OK : E_CUDA;
+  if (e3 != cudaSuccess || e2 != cudaSuccess) return E_CUDA;
+  // k_check is a grid-stride loop: one resident wave avoids a ragged second
+  int dev = 0, sms = 0, b3 = 0, b2 = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_check<3>, 128, 4 * sizeof(WarpCommit<3>)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_check<2>, 128, 4 * sizeof(WarpCommit<2>)) != cudaSuccess)
+    return E_CUDA;
+  g_check_wave[1] = std::max(1, sms * b3);
+  g_check_wave[0] = std::max(1, sms * b2);
+  return E_OK;
 }
 
 void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, const Feed& fd, Prof* pf) {
