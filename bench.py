@@ -55,6 +55,12 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_POINTS)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--workload", default="c2", choices=["c2", "c4", "c5"],
+                   help="c2: 1M-point 3D build (the headline line); c4: 4,096 sets batched vs one set per "
+                        "launch; c5: Poisson request stream through the serving loop")
+    p.add_argument("--requests", type=int, default=20_000, help="c5: requests in the stream")
+    p.add_argument("--slots", type=int, default=3, help="c5: server slots")
+    p.add_argument("--max-batch-points", type=int, default=2_000_000, help="c5: largest batch a slot forms")
     return p.parse_args()
 
 
@@ -174,6 +180,207 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_c4(args):
+    """4,096 independent 3D sets (log-uniform 32..65,536 points): one batched
+    build per step against one build per set, same GPU, same outputs."""
+    import torch
+    from voronoids_gb300 import _native
+    from voronoids_gb300 import workloads as W
+    L = _native.load()
+    pts_h, off = W.c4_sets()
+    n, nsets = int(off[-1]), len(off) - 1
+    pts_d = torch.from_numpy(pts_h).cuda()
+    cap = 9 * n
+    uv_d = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    st = ctypes.c_int(0)
+    tree = ctypes.c_void_p(L.vd_tree_create(3, ctypes.c_void_p(stream.cuda_stream), ctypes.byref(st)))
+    eoff = np.zeros(nsets + 1, dtype=np.int64)
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    offp = off.astype(np.int64)
+
+    def batched():
+        rc = L.vd_batch_delaunay_device(tree, ctypes.c_void_p(pts_d.data_ptr()), offp.ctypes.data_as(i64p), nsets,
+                                        SEED, ctypes.c_void_p(uv_d.data_ptr()), cap, eoff.ctypes.data_as(i64p))
+        if rc not in (0, 4):
+            raise SystemExit(f"vd_batch_delaunay_device failed: {rc}")
+
+    for _ in range(max(args.warmup, 3)):
+        batched()
+    clk = Clocks(0)
+    clk.start()
+    times = []
+    launches0 = L.vd_kernel_launches()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batched()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    launches = (L.vd_kernel_launches() - launches0) // max(args.steps, 1)
+    clocks = clk.stop()
+    ok = ctypes.c_int(0)
+    L.vd_check_delaunay(tree, ctypes.byref(ok), None)
+    ms = float(np.mean(times))
+    # end to end: host points in, host edges out (vd_batch_delaunay)
+    pts_pin = torch.from_numpy(pts_h).pin_memory()
+    uv_pin = torch.empty((cap, 2), dtype=torch.int32).pin_memory()
+    hp = ctypes.cast(ctypes.c_void_p(pts_pin.data_ptr()), ctypes.POINTER(ctypes.c_double))
+    etimes = []
+    for _ in range(max(1, args.steps // 2)):
+        t0 = time.perf_counter()
+        rc = L.vd_batch_delaunay(tree, hp, offp.ctypes.data_as(i64p), nsets, SEED,
+                                 ctypes.c_void_p(uv_pin.data_ptr()), cap, eoff.ctypes.data_as(i64p))
+        etimes.append(time.perf_counter() - t0)
+    ems = 1e3 * float(np.mean(etimes))
+    ref_edges = uv_d[: int(eoff[-1])].clone()
+    ref_eoff = eoff.copy()
+    # one set per launch on a second tree, compared set by set
+    t2 = ctypes.c_void_p(L.vd_tree_create(3, ctypes.c_void_p(stream.cuda_stream), ctypes.byref(st)))
+    out2 = torch.empty((9 * 65536 + 1024, 2), dtype=torch.int32, device="cuda")
+    m = ctypes.c_int64(0)
+    L.vd_delaunay_device(t2, ctypes.c_void_p(pts_d.data_ptr()), int(off[1]), SEED, ctypes.c_void_p(out2.data_ptr()),
+                         out2.shape[0], ctypes.byref(m))
+    mismatch = 0
+    one_ms = 0.0
+    for s in range(nsets):
+        a, b = int(off[s]), int(off[s + 1])
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rc = L.vd_delaunay_device(t2, ctypes.c_void_p(pts_d.data_ptr() + 24 * a), b - a, SEED,
+                                  ctypes.c_void_p(out2.data_ptr()), out2.shape[0], ctypes.byref(m))
+        e1.record(stream)
+        e1.synchronize()
+        one_ms += e0.elapsed_time(e1)
+        if rc not in (0, 4) or m.value != ref_eoff[s + 1] - ref_eoff[s] or \
+                not torch.equal(out2[: m.value], ref_edges[ref_eoff[s]:ref_eoff[s + 1]]):
+            mismatch += 1
+    L.vd_tree_free(t2)
+    L.vd_tree_free(tree)
+    line = {
+        "metric": "Mpts/s batched build, 4,096 3D sets", "value": round(n / (ms / 1e3) / 1e6, 4), "unit": "Mpts/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "4,096 independent 3D sets, sizes floor(exp(U(ln 32, ln 65536))), uniform [0,1)^3 "
+                               "(splitmix64 seed 0xD1A00004), one batched build per step", "points": n,
+                   "sets": nsets, "l2": "flushed between steps (256 MB write)"},
+        "one_set_per_launch": {"value": round(n / (one_ms / 1e3) / 1e6, 4), "unit": "Mpts/s",
+                               "ms_total": round(one_ms, 1), "mismatching_sets": mismatch},
+        "batched_over_one_set_per_launch": round(one_ms / ms, 2),
+        "validator_ok": bool(ok.value), "edges": int(ref_eoff[-1]), "clocks": clocks, "gpu_launches": int(launches),
+        "e2e": {"value": round(n / (ems / 1e3) / 1e6, 4), "unit": "Mpts/s", "h2d_bytes_per_step": int(n * 24),
+                "d2h_bytes_per_step": int(ref_eoff[-1] * 8), "ms_per_step": round(ems, 3)},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_c5(args):
+    """Poisson stream of triangulation requests (2D/3D 50/50, log-uniform
+    100..200,000 points) through the serving loop at 80% of its measured
+    capacity; latency from submission to completion."""
+    from voronoids_gb300 import _native
+    from voronoids_gb300 import workloads as W
+    L = _native.load()
+    reqs = W.c5_requests(args.requests)
+    mean_pts = float(np.mean([r[1] for r in reqs]))
+    budget = 64 << 30
+    i64p = ctypes.POINTER(ctypes.c_int64)
+
+    def serve(stream_reqs, arrivals):
+        st = ctypes.c_int(0)
+        srv = ctypes.c_void_p(L.vd_server_new(budget, args.slots, args.max_batch_points, SEED, ctypes.byref(st)))
+        if st.value != 0:
+            raise SystemExit(f"vd_server_new failed: {st.value}")
+        nreq = len(stream_reqs)
+        sub_t = np.zeros(nreq)
+        done_t = np.zeros(nreq)
+        lag = np.zeros(nreq)
+        statuses = np.zeros(nreq, dtype=np.int64)
+        id_of = {}
+        uv = np.empty(2 * (10 * 200_000 + 64), dtype=np.uint32)
+        finished = [0]
+        t_start = time.perf_counter()
+
+        def poller():
+            ids = np.zeros(4096, dtype=np.int64)
+            m = ctypes.c_int64(0)
+            ne = ctypes.c_int64(0)
+            rs = ctypes.c_int(0)
+            while finished[0] < nreq:
+                L.vd_server_poll(srv, ids.ctypes.data_as(i64p), 4096, ctypes.byref(m), 5)
+                now = time.perf_counter() - t_start
+                for rid in ids[: m.value].tolist():
+                    k = id_of.get(rid)
+                    while k is None:  # submit() has not recorded it yet
+                        time.sleep(0.0001)
+                        k = id_of.get(rid)
+                    done_t[k] = now
+                    L.vd_server_result(srv, rid, ctypes.c_void_p(uv.ctypes.data), len(uv) // 2, ctypes.byref(ne),
+                                       ctypes.byref(rs))
+                    statuses[k] = rs.value
+                    finished[0] += 1
+
+        th = threading.Thread(target=poller, daemon=True)
+        th.start()
+        rid = ctypes.c_int64(0)
+        for k, r in enumerate(stream_reqs):
+            p = W.c5_points(r)
+            if arrivals is not None:
+                wait = arrivals[k] - (time.perf_counter() - t_start)
+                if wait > 0:
+                    time.sleep(wait)
+            now = time.perf_counter() - t_start
+            lag[k] = now - (arrivals[k] if arrivals is not None else 0.0)
+            sub_t[k] = now
+            rc = L.vd_server_submit(srv, r[0], p.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), r[1],
+                                    ctypes.byref(rid))
+            if rc != 0:
+                raise SystemExit(f"vd_server_submit failed: {rc}")
+            id_of[rid.value] = k
+        th.join()
+        stats = np.zeros(8, dtype=np.int64)
+        L.vd_server_stats(srv, stats.ctypes.data_as(i64p))
+        L.vd_server_free(srv)
+        return sub_t, done_t, lag, statuses, stats
+
+    # capacity: a closed burst of the first requests
+    ncap = min(2000, len(reqs))
+    sub_t, done_t, _, _, _ = serve(reqs[:ncap], None)
+    cap_pts = sum(r[1] for r in reqs[:ncap]) / (done_t.max() - sub_t.min())
+    rate = 0.8 * cap_pts / mean_pts  # requests per second
+    gaps = np.random.default_rng(SEED).exponential(1.0 / rate, len(reqs))
+    arrivals = np.cumsum(gaps) - gaps[0]
+    clk = Clocks(0)
+    clk.start()
+    sub_t, done_t, lag, statuses, stats = serve(reqs, arrivals)
+    clocks = clk.stop()
+    lat = 1e3 * (done_t - sub_t)
+    total = sum(r[1] for r in reqs)
+    span = done_t.max() - sub_t.min()
+    line = {
+        "metric": "served Mpts/s with p50/p99 latency, Poisson request stream", "value": round(total / span / 1e6, 4),
+        "unit": "Mpts/s", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": round(1e3 * span, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{len(reqs)} requests, 2D/3D 50/50, sizes log-uniform 100..200,000 points uniform "
+                               f"in the unit square/cube (splitmix64 seed 0xD1A00005), Poisson arrivals at 80% of "
+                               f"the measured capacity", "points": int(total), "slots": args.slots,
+                   "max_batch_points": args.max_batch_points, "pool_budget_bytes": budget},
+        "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 2), "p99": round(float(np.percentile(lat, 99)), 2),
+                       "mean": round(float(lat.mean()), 2), "max": round(float(lat.max()), 2)},
+        "capacity_mpts_s": round(cap_pts / 1e6, 4), "arrival_rate_req_s": round(rate, 2),
+        "submission_lag_ms_p99": round(1e3 * float(np.percentile(lag, 99)), 2),
+        "failed_requests": int(np.count_nonzero(statuses)),
+        "server": {"batches": int(stats[2]), "peak_bytes_in_flight": int(stats[4]), "isolated": int(stats[6])},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -181,6 +388,12 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.workload == "c4":
+        run_c4(args)
+        return
+    if args.workload == "c5":
+        run_c5(args)
         return
 
     import torch
@@ -329,7 +542,7 @@ def main():
                                    "input-index edge list", "points": n,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "flushed between steps (256 MB write)", "edges": edges,
-                       "tuning": "3D defaults: 2 resolution passes, thinning radius 2, prefixes 64 x4"},
+                       "tuning": "3D defaults: 2 resolution passes, thinning radius 2, priority levels 64 x1.25 fed at 0.12 x inserted, rounds replayed as CUDA graphs"},
             "clocks": clocks, "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
             "cpu_baseline": cpu,
             "build_stats": {k: stats[k] for k in ("rounds", "inserted", "max_cavity", "pred_f32", "pred_f64",

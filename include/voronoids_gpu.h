@@ -213,6 +213,34 @@ int vd_num_sets(vd_tree* t, int* nsets);
  * or vd_delaunay_tree / vd_delaunay_device. */
 vd_tree* vd_tree_create(int dim, void* stream, int* status);
 
+/* Serving loop (no reference counterpart: the reference triangulates one set
+ * per blocking call, src/lib.rs:104-125).  Requests of mixed size and
+ * dimension are queued by vd_server_submit (points copied).  `slots` workers,
+ * each with its own host thread, CUDA stream and reusable trees, form batches
+ * from the queue of the dimension whose oldest request waited longest and run
+ * them as batched builds, so that requests arriving while others run are
+ * admitted as slots and budget free up, and batches of different slots
+ * overlap on the device.  Admission: the estimated device bytes of the
+ * requests in flight (3D 360 B/point, 2D 100 B/point, 1.5x slack included)
+ * stay within `pool_bytes`; a request larger than the budget finishes with
+ * VD_ERR_NOMEM.  `max_batch_points` caps a batch (0 = only the budget).
+ * Each result is the triangulation of the request alone. */
+typedef struct vd_server vd_server;
+vd_server* vd_server_new(uint64_t pool_bytes, int slots, int64_t max_batch_points, uint64_t seed, int* status);
+int vd_server_submit(vd_server* s, int dim, const double* pts, int64_t n, int64_t* id);
+/* Ids of requests finished since the last call (at most `cap`); waits up to
+ * `timeout_ms` for one when none is ready. */
+int vd_server_poll(vd_server* s, int64_t* ids, int64_t cap, int64_t* n, int timeout_ms);
+/* Result of a finished request: its status and edges (uint32 pairs numbered
+ * within the request, sorted).  With `uv` NULL only the count and status are
+ * returned; otherwise the result is copied out and released. */
+int vd_server_result(vd_server* s, int64_t id, uint32_t* uv, int64_t cap, int64_t* n_edges, int* req_status);
+/* out[0..7]: submitted, finished, batches, bytes in flight, peak bytes in
+ * flight, queued, requests re-run alone after a failed batch, budget. */
+int vd_server_stats(vd_server* s, int64_t* out);
+/* Finishes every queued request, then stops the workers. */
+void vd_server_free(vd_server* s);
+
 /* Sorted edge list of a caller-owned simplex list, for callers that may not
  * allocate GPU memory (for example an application whose memory manager owns
  * the whole device, or a loop that cannot afford the synchronisation of a

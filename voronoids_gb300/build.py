@@ -21,7 +21,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvoronoids_gpu.so")
 HOSTLIB = os.path.join(HERE, "libvd_pred_host.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["vd_build.cu", "vd_edges.cu", "vd_check.cu", "vd_size.cu", "vd_noalloc.cu", "vd_capi.cu"]
+SOURCES = ["vd_build.cu", "vd_edges.cu", "vd_check.cu", "vd_size.cu", "vd_noalloc.cu", "vd_capi.cu", "vd_server.cu"]
 HEADERS = ["vd_common.cuh", "vd_predicates.cuh"]
 
 
@@ -74,7 +74,7 @@ def build(force=False, verbose=False, ptxas_info=False):
                     raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + f".tmp{os.getpid()}"
-        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

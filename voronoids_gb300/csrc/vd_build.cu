@@ -34,6 +34,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "vd_common.cuh"
 
@@ -1295,7 +1296,8 @@ void launch_levels(const DevTree& T, const Launch& L, int64_t n, int base_vid, u
   k_level_order<<<L.blocks, 256, 0, L.stream>>>(T, n, base_vid, seed, th, d_work + kMaxLevels);
 }
 
-int prepare_round_kernels() {
+namespace {
+int prepare_once() {
   const cudaError_t e3 = cudaFuncSetAttribute(k_check<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               4 * (int)sizeof(WarpCommit<3>));
   const cudaError_t e2 = cudaFuncSetAttribute(k_check<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1311,6 +1313,15 @@ int prepare_round_kernels() {
   g_check_wave[1] = std::max(1, sms * b3);
   g_check_wave[0] = std::max(1, sms * b2);
   return E_OK;
+}
+}  // namespace
+
+// Once per process (trees may be created from several host threads).
+int prepare_round_kernels() {
+  static std::once_flag once;
+  static int rc = E_CUDA;
+  std::call_once(once, [] { rc = prepare_once(); });
+  return rc;
 }
 
 void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, const Feed& fd, Prof* pf) {

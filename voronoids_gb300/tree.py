@@ -308,3 +308,62 @@ def delaunay_batch(point_sets, seed=0, tree=None):
         if tree is None:
             t.close()
     return [uv[eoff[s]:eoff[s + 1]].astype(np.int64) for s in range(len(sets))]
+
+
+class Server:
+    """Continuous-batching triangulation server (``vd_server_*``).
+
+    ``submit(points)`` queues a request and returns its id; ``poll()`` returns
+    the ids finished since the last call; ``result(id)`` returns the sorted
+    (m, 2) int64 edge array of a finished request (numbered within it)."""
+
+    def __init__(self, pool_bytes=64 << 30, slots=2, max_batch_points=0, seed=0):
+        L = _native.load()
+        st = ctypes.c_int(0)
+        h = L.vd_server_new(int(pool_bytes), int(slots), int(max_batch_points), int(seed), ctypes.byref(st))
+        if not h or st.value != _native.VD_OK:
+            raise VDError(st.value or 3, "vd_server_new")
+        self._h = ctypes.c_void_p(h)
+
+    def submit(self, points):
+        p = _points(points)
+        i = ctypes.c_int64(0)
+        _check(_native.load().vd_server_submit(self._h, p.shape[1], _dp(p), p.shape[0], ctypes.byref(i)), "submit")
+        return i.value
+
+    def poll(self, timeout_ms=0, cap=4096):
+        ids = np.zeros(cap, dtype=np.int64)
+        n = ctypes.c_int64(0)
+        _check(_native.load().vd_server_poll(self._h, ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), cap,
+                                             ctypes.byref(n), int(timeout_ms)), "poll")
+        return ids[: n.value].tolist()
+
+    def result(self, rid):
+        L = _native.load()
+        m = ctypes.c_int64(0)
+        st = ctypes.c_int(0)
+        _check(L.vd_server_result(self._h, rid, None, 0, ctypes.byref(m), ctypes.byref(st)), "result")
+        uv = np.zeros((m.value, 2), dtype=np.uint32)
+        _check(L.vd_server_result(self._h, rid, uv.ctypes.data_as(ctypes.c_void_p), m.value, ctypes.byref(m),
+                                  ctypes.byref(st)), "result")
+        if st.value != _native.VD_OK:
+            raise VDError(st.value, f"request {rid}")
+        return uv.astype(np.int64)
+
+    def stats(self):
+        out = np.zeros(8, dtype=np.int64)
+        _check(_native.load().vd_server_stats(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))), "stats")
+        keys = ("submitted", "finished", "batches", "bytes_in_flight", "peak_bytes_in_flight", "queued",
+                "isolated", "budget")
+        return dict(zip(keys, out.tolist()))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.load().vd_server_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

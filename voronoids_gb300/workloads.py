@@ -99,3 +99,18 @@ def lattice_points(side, dim, jitter=0.0, seed=7):
     if jitter:
         g = g + (uniform01(seed, g.size).reshape(g.shape) * 2 - 1) * jitter
     return g
+
+
+def c5_requests(nreq=20_000, lo=100, hi=200_000, seed=None):
+    """Serving stream: per request (dim, n, point seed); dims 2/3 at 50/50,
+    sizes floor(exp(U(ln lo, ln hi)))."""
+    seed = config_seed(5) if seed is None else seed
+    u = uniform01(seed, 2 * nreq).reshape(nreq, 2)
+    dims = np.where(u[:, 0] < 0.5, 2, 3)
+    sizes = np.floor(np.exp(np.log(lo) + u[:, 1] * (np.log(hi) - np.log(lo)))).astype(np.int64)
+    return [(int(d), int(n), seed * 1_000_003 + i) for i, (d, n) in enumerate(zip(dims, sizes))]
+
+
+def c5_points(req):
+    dim, n, s = req
+    return uniform_points(n, dim, s)
