@@ -15,8 +15,9 @@ sizing, round-parallel insertion of every point, sorted edge list.
           build's stream during a second timed region of K steps).
 
 Between timed steps the L2 (129 MB) is flushed by writing a 256 MB buffer.
-`--impl reference` times the CPU restatement of the reference path
-(oracle/, sequential exact Bowyer-Watson) on a bounded sample.
+`--impl reference` times the reference's parallel CPU path, restated in C++
+(oracle/: 1e5 sequential inserts, then 2-ring queue, greedy rounds and
+per-round parallel updates on all host threads), on a bounded sample.
 """
 import argparse
 import ctypes
@@ -36,7 +37,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Mpts/s 3D 1M exact graph"
 N_POINTS = 1_000_000
 SEED = 0x5EED
-CPU_SAMPLE = 100_000
+CPU_SAMPLE = 200_000
 
 # Algorithmic bytes per unit: k_cavity moves one 32-byte
 # simplex record and four 32-byte split-coordinate records per conflict test;
@@ -137,33 +138,47 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def cpu_baseline():
-    """The oracle (sequential exact Bowyer-Watson, one thread) on a bounded sample."""
+CPU_PREFIX = 100_000  # points the reference inserts one at a time first (src/lib.rs:108)
+
+
+def cpu_threads():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def cpu_sample_desc(threads):
+    return (f"{CPU_SAMPLE} points of the same uniform 3D distribution per step: the reference's parallel path "
+            f"restated in C++ (oracle/, not the crate: no Rust toolchain here) on {threads} host threads -- "
+            f"the first {CPU_PREFIX} points inserted one at a time as src/lib.rs:108-114 does, the rest through "
+            f"2-ring queue, greedy round placement and per-round parallel updates (src/scheduler.rs, "
+            f"src/delaunay_tree.rs:336-386), exact predicates, sorted edge list")
+
+
+def cpu_build(p, threads):
     from oracle import oracle as O
-    from voronoids_gb300 import workloads as W
-    p = W.uniform_points(CPU_SAMPLE, 3, W.config_seed(2))
     t0 = time.perf_counter()
-    tri = O.Triangulation(p, seed=SEED)
+    tri = O.Triangulation(p, seed=SEED, threads=threads, prefix=CPU_PREFIX)
     _ = tri.edges()
-    dt = time.perf_counter() - t0
-    return {"value": round(CPU_SAMPLE / dt / 1e6, 4), "unit": "Mpts/s", "cores": 1, "kind": "port",
-            "sample": f"{CPU_SAMPLE} points of the same uniform 3D distribution, sequential exact "
-                      f"Bowyer-Watson restatement of the reference path (oracle/), sorted edge list"}
+    return time.perf_counter() - t0
+
+
+def cpu_baseline():
+    """The reference's parallel CPU path (C++ restatement, all host threads) on a bounded sample."""
+    from voronoids_gb300 import workloads as W
+    threads = cpu_threads()
+    dt = cpu_build(W.uniform_points(CPU_SAMPLE, 3, W.config_seed(2)), threads)
+    return {"value": round(CPU_SAMPLE / dt / 1e6, 4), "unit": "Mpts/s", "cores": threads, "kind": "port",
+            "sample": cpu_sample_desc(threads)}
 
 
 def run_reference(args, rank):
     if rank != 0:
         return
-    from oracle import oracle as O
     from voronoids_gb300 import workloads as W
+    threads = cpu_threads()
     p = W.uniform_points(CPU_SAMPLE, 3, W.config_seed(2))
     for _ in range(args.warmup):
-        O.Triangulation(p[:10_000], seed=SEED).edges()
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        O.Triangulation(p, seed=SEED).edges()
-        times.append(time.perf_counter() - t0)
+        cpu_build(p[:20_000], threads)
+    times = [cpu_build(p, threads) for _ in range(args.steps)]
     ms = 1e3 * float(np.mean(times))
     v = CPU_SAMPLE / (ms / 1e3) / 1e6
     line = {
@@ -172,9 +187,8 @@ def run_reference(args, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"uniform 3D points in [0,1)^3, seeded; bounded CPU sample of {CPU_SAMPLE} "
                                f"(the GPU arm triangulates {args.n})", "points": CPU_SAMPLE},
-        "cpu_baseline": {"value": round(v, 4), "unit": "Mpts/s", "cores": 1, "kind": "port",
-                         "sample": f"{CPU_SAMPLE} points per step; the reference crate (Rust) cannot be built "
-                                   f"here, so its path is timed as the oracle/ restatement"},
+        "cpu_baseline": {"value": round(v, 4), "unit": "Mpts/s", "cores": threads, "kind": "port",
+                         "sample": cpu_sample_desc(threads)},
         "e2e": {"value": round(v, 4), "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -199,6 +213,15 @@ def run_c4(args):
     eoff = np.zeros(nsets + 1, dtype=np.int64)
     i64p = ctypes.POINTER(ctypes.c_int64)
     offp = off.astype(np.int64)
+
+    # autotune launch shape and round settings on a 2M-point sample of the sets
+    tuned = np.zeros(8, dtype=np.int64)
+    rc = L.vd_autotune_batch(tree, ctypes.c_void_p(pts_d.data_ptr()), offp.ctypes.data_as(i64p), nsets, 2_000_000,
+                             tuned.ctypes.data_as(i64p))
+    if rc not in (0, 4):
+        raise SystemExit(f"vd_autotune_batch failed: {rc}")
+    tuned = dict(zip(("warps_per_sm", "blocks_per_sm", "passes", "thin", "ratio_x1000", "sample_us",
+                      "sample_points", "sample_sets"), tuned.tolist()))
 
     def batched():
         rc = L.vd_batch_delaunay_device(tree, ctypes.c_void_p(pts_d.data_ptr()), offp.ctypes.data_as(i64p), nsets,
@@ -271,7 +294,7 @@ def run_c4(args):
                    "sets": nsets, "l2": "flushed between steps (256 MB write)"},
         "one_set_per_launch": {"value": round(n / (one_ms / 1e3) / 1e6, 4), "unit": "Mpts/s",
                                "ms_total": round(one_ms, 1), "mismatching_sets": mismatch},
-        "batched_over_one_set_per_launch": round(one_ms / ms, 2),
+        "batched_over_one_set_per_launch": round(one_ms / ms, 2), "autotuned": tuned,
         "validator_ok": bool(ok.value), "edges": int(ref_eoff[-1]), "clocks": clocks, "gpu_launches": int(launches),
         "e2e": {"value": round(n / (ems / 1e3) / 1e6, 4), "unit": "Mpts/s", "h2d_bytes_per_step": int(n * 24),
                 "d2h_bytes_per_step": int(ref_eoff[-1] * 8), "ms_per_step": round(ems, 3)},

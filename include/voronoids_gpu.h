@@ -207,6 +207,20 @@ int vd_batch_delaunay(vd_tree* t, const double* pts, const int64_t* offsets, int
 /* Device points in, device pairs out (`offsets` and `edge_offsets` on the host). */
 int vd_batch_delaunay_device(vd_tree* t, const double* d_pts, const int64_t* offsets, int nsets, uint64_t seed,
                              uint32_t* d_uv, int64_t cap, int64_t* edge_offsets);
+/* Launch shape of the round kernels: warps per SM for the candidate-per-warp
+ * kernels (4..32, multiple of 4; default 20) and 256-thread blocks per SM for
+ * the point-per-thread kernels (1..32; default 8).  No reference counterpart. */
+int vd_set_launch(vd_tree* t, int warps_per_sm, int blocks_per_sm);
+/* Autotuner for batched builds (no reference counterpart).  Times batched
+ * builds of a sample of the sets (every k-th set, about `sample_points`
+ * points: the batch's size mix) with CUDA events, sweeping in turn the feed
+ * ratio, resolution passes, thinning radius, warps per SM and blocks per SM,
+ * and keeps the fastest setting on the tree.  out (NULL or 8 entries): warps
+ * per SM, blocks per SM, passes, thinning radius, ratio x 1000, best sample
+ * microseconds, sample points, sample sets.  The tree is left reset to the
+ * sample. */
+int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, int nsets, int64_t sample_points,
+                      int64_t* out);
 /* Point sets of the tree (1 unless built by vd_batch_*). */
 int vd_num_sets(vd_tree* t, int* nsets);
 /* An empty tree (no super simplex yet) for the batched calls, vd_tree_reset

@@ -36,6 +36,10 @@ def lib():
         L.vdo_build.argtypes = [ctypes.c_int, dp, ctypes.c_int64, ctypes.c_uint64,
                                 ctypes.POINTER(ctypes.c_int)]
         L.vdo_build.restype = ctypes.c_void_p
+        L.vdo_build_parallel.argtypes = [ctypes.c_int, dp, ctypes.c_int64, ctypes.c_uint64, ctypes.c_int,
+                                         ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]
+        L.vdo_build_parallel.restype = ctypes.c_void_p
+        L.vdo_parallel_rounds.restype = ctypes.c_int
         L.vdo_free.argtypes = [ctypes.c_void_p]
         L.vdo_num_duplicates.argtypes = [ctypes.c_void_p]
         L.vdo_num_duplicates.restype = ctypes.c_int64
@@ -127,12 +131,19 @@ class Triangulation:
     """Sequential exact Bowyer-Watson over `points` (super simplex sized
     from the same points, as ``voronoids.delaunay`` does)."""
 
-    def __init__(self, points, seed=0):
+    def __init__(self, points, seed=0, threads=0, prefix=100_000):
+        """threads > 0: the reference's parallel path (sequential `prefix`
+        points, then 2-ring queue, greedy rounds and per-round parallel
+        updates on `threads` host threads); same triangulation."""
         p = _c(points, np.float64)
         self.dim = p.shape[1]
         self.n = p.shape[0]
         st = ctypes.c_int(0)
-        self._h = lib().vdo_build(self.dim, _dp(p), self.n, seed, ctypes.byref(st))
+        if threads > 0:
+            self._h = lib().vdo_build_parallel(self.dim, _dp(p), self.n, seed, int(threads), int(prefix),
+                                               ctypes.byref(st))
+        else:
+            self._h = lib().vdo_build(self.dim, _dp(p), self.n, seed, ctypes.byref(st))
         self.status = st.value
 
     def __del__(self):

@@ -38,7 +38,12 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
 #include <map>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -630,6 +635,395 @@ int insert_vertex(Tree& t, int vid) {
   return OK;
 }
 
+// Duplicate groups: of equal points the one with the smallest priority is
+// kept; dup_of[k] = kept input index for the others.
+void mark_duplicates(Tree& t, int64_t n, uint64_t seed) {
+  // duplicate groups: keep the smallest priority
+  t.dup_of.assign(n, -1);
+  {
+    struct K {
+      double x, y, z;
+      bool operator==(const K& o) const { return x == o.x && y == o.y && z == o.z; }
+    };
+    struct H {
+      size_t operator()(const K& k) const {
+        uint64_t a, b, c;
+        memcpy(&a, &k.x, 8);
+        memcpy(&b, &k.y, 8);
+        memcpy(&c, &k.z, 8);
+        return (size_t)(a * 0x9E3779B97F4A7C15ULL ^ (b + 0x632BE59BD9B4E019ULL) * 31 ^ c);
+      }
+    };
+    std::unordered_map<K, int64_t, H> best;
+    best.reserve(n * 2);
+    for (int64_t k = 0; k < n; ++k) {
+      const P3& p = t.pts[t.ns + k];
+      K key{p.x == 0.0 ? 0.0 : p.x, p.y == 0.0 ? 0.0 : p.y, p.z == 0.0 ? 0.0 : p.z};
+      auto it = best.find(key);
+      if (it == best.end()) {
+        best.emplace(key, k);
+      } else {
+        int64_t j = it->second;
+        uint32_t pk = priority((uint32_t)(t.ns + k), seed), pj = priority((uint32_t)(t.ns + j), seed);
+        if (pk < pj) {
+          t.dup_of[j] = (int)k;
+          it->second = k;
+        } else {
+          t.dup_of[k] = (int)j;
+        }
+      }
+    }
+    // resolve chains to the final kept index
+    for (int64_t k = 0; k < n; ++k) {
+      if (t.dup_of[k] < 0) continue;
+      const P3& p = t.pts[t.ns + k];
+      K key{p.x == 0.0 ? 0.0 : p.x, p.y == 0.0 ? 0.0 : p.y, p.z == 0.0 ? 0.0 : p.z};
+      t.dup_of[k] = (int)best[key];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Parallel path of the reference, restated with std::thread for the CPU
+// baseline: src/lib.rs:104-125 (the first 1e5 points one at a time, the rest
+// through add_points_to_tree), src/delaunay_tree.rs:336-386 (queue,
+// placement, then per round TreeUpdate::new in parallel and one apply),
+// src/scheduler.rs:6-28 (queue entry: located conflict region and its
+// 2-ring of simplex ids) and :30-55 (greedy round = 1 + round of the
+// previous point sharing a 2-ring simplex).  Apply checks that an update's
+// conflict region and outer shell are unchanged since it was computed (the
+// placement is made on the tree before the rounds); a stale update is
+// recomputed on the spot, so the result is the exact triangulation.
+// ---------------------------------------------------------------------------
+struct Update {
+  int vid = -1;
+  std::vector<int> cav;
+  struct Facet {
+    int simp, face, outer;
+  };
+  std::vector<Facet> bnd;
+  int status = OK;
+};
+
+// Persistent worker pool (the role rayon's global pool plays in the
+// reference): run(n, fn) calls fn(i, tid) for i < n on all threads.
+class Pool {
+ public:
+  explicit Pool(int threads) : threads_(std::max(1, threads)) {
+    for (int k = 1; k < threads_; ++k) workers_.emplace_back([this, k] { loop(k); });
+  }
+  ~Pool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      quit_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& w : workers_) w.join();
+  }
+  int threads() const { return threads_; }
+  template <class F>
+  void run(int64_t n, F&& fn) {
+    if (n <= 0) return;
+    std::function<void(int64_t, int)> job = fn;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      job_ = &job;
+      n_ = n;
+      next_.store(0);
+      busy_ = threads_ - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    work(0);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return busy_ == 0; });
+    job_ = nullptr;
+  }
+
+ private:
+  void work(int tid) {
+    const int64_t grain = std::max<int64_t>(1, n_ / (16 * threads_));
+    for (;;) {
+      const int64_t b = next_.fetch_add(grain);
+      if (b >= n_) break;
+      const int64_t e = std::min<int64_t>(n_, b + grain);
+      for (int64_t i = b; i < e; ++i) (*job_)(i, tid);
+    }
+  }
+  void loop(int tid) {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (quit_) return;
+      }
+      work(tid);
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        --busy_;
+      }
+      done_cv_.notify_all();
+    }
+  }
+  int threads_;
+  std::vector<std::thread> workers_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_cv_;
+  std::function<void(int64_t, int)>* job_ = nullptr;
+  int64_t n_ = 0;
+  std::atomic<int64_t> next_{0};
+  int busy_ = 0;
+  uint64_t gen_ = 0;
+  bool quit_ = false;
+};
+
+// Read-only visibility walk (no counters touched).
+int locate_ro(const Tree& t, const P3& p, int start, long long* nexact) {
+  int cur = start;
+  const long long cap = 64 + 4 * (long long)t.s.size();
+  for (long long step = 0; step < cap; ++step) {
+    int nv = t.dim + 1, moved = -1;
+    for (int j = 0; j < nv; ++j) {
+      P3 q[4];
+      simplex_points(t, cur, q);
+      q[j] = p;
+      if (orient(t.dim, q, nexact) < 0) {
+        moved = j;
+        break;
+      }
+    }
+    if (moved < 0) return cur;
+    const int nb = t.s[cur].n[moved];
+    if (nb < 0) return -2;
+    cur = nb;
+  }
+  return -1;
+}
+
+// TreeUpdate::new (src/delaunay_tree.rs:709-740): conflict region and its
+// boundary facets of vertex vid against the current tree, read-only.
+void compute_update(const Tree& t, int vid, int start, Update& u, long long* nexact) {
+  u.vid = vid;
+  u.cav.clear();
+  u.bnd.clear();
+  u.status = OK;
+  const P3 p = t.pts[vid];
+  const int nv = t.dim + 1;
+  long long nsos = 0;
+  const int c0 = locate_ro(t, p, start, nexact);
+  if (c0 < 0) {
+    u.status = c0 == -2 ? ERR_OUTSIDE : ERR_WALK;
+    return;
+  }
+  u.cav.push_back(c0);
+  for (size_t h = 0; h < u.cav.size(); ++h) {
+    const int c = u.cav[h];
+    for (int f = 0; f < nv; ++f) {
+      const int nb = t.s[c].n[f];
+      if (nb < 0) {
+        u.bnd.push_back({c, f, -1});
+        continue;
+      }
+      if (std::find(u.cav.begin(), u.cav.end(), nb) != u.cav.end()) continue;
+      P3 q[4];
+      simplex_points(t, nb, q);
+      int key[4];
+      for (int i = 0; i < nv; ++i) key[i] = t.s[nb].v[i];
+      if (insphere_sos(t.dim, q, key, p, vid, nexact, &nsos) > 0)
+        u.cav.push_back(nb);
+      else
+        u.bnd.push_back({c, f, nb});
+    }
+  }
+}
+
+// insert_point (src/delaunay_tree.rs:125-211) of a computed update: star of
+// new simplices, one per boundary facet, stitched by shared ridges.
+void apply_update(Tree& t, const Update& u) {
+  const int nv = t.dim + 1;
+  const int base = (int)t.s.size();
+  t.s.resize(base + u.bnd.size());
+  std::map<std::array<int, 2>, std::pair<int, int>> open;
+  for (size_t k = 0; k < u.bnd.size(); ++k) {
+    const Update::Facet& F = u.bnd[k];
+    Simplex ns;
+    ns.alive = true;
+    for (int i = 0; i < 4; ++i) {
+      ns.v[i] = (i < nv) ? t.s[F.simp].v[i] : -1;
+      ns.n[i] = -1;
+    }
+    ns.v[F.face] = u.vid;
+    ns.n[F.face] = F.outer;
+    const int id = base + (int)k;
+    if (F.outer >= 0) {
+      Simplex& O = t.s[F.outer];
+      for (int j = 0; j < nv; ++j)
+        if (O.n[j] == F.simp) O.n[j] = id;
+    }
+    for (int g = 0; g < nv; ++g) {
+      if (g == F.face) continue;
+      std::array<int, 2> ridge = {-1, -1};
+      int r = 0;
+      for (int i = 0; i < nv; ++i)
+        if (i != g && i != F.face) ridge[r++] = ns.v[i];
+      if (r == 2 && ridge[0] > ridge[1]) std::swap(ridge[0], ridge[1]);
+      auto it = open.find(ridge);
+      if (it == open.end()) {
+        open[ridge] = {id, g};
+      } else {
+        ns.n[g] = it->second.first;
+        t.s[it->second.first].n[it->second.second] = id;
+        open.erase(it);
+      }
+    }
+    t.s[id] = ns;
+  }
+  for (int c : u.cav) t.s[c].alive = false;
+  t.last = base;
+}
+
+// Location hints: a coarse grid over the super simplex's bounding box, each
+// cell holding a live simplex near it (the reference starts its search at
+// the kd-tree nearest vertex, src/delaunay_tree.rs:35-40).
+struct Grid {
+  double lo[3], inv[3];
+  int side = 1;
+  std::vector<int> cell;
+  int index(const P3& p, int dim) const {
+    const double c[3] = {p.x, p.y, p.z};
+    int idx = 0;
+    for (int k = dim - 1; k >= 0; --k) {
+      int i = (int)((c[k] - lo[k]) * inv[k] * side);
+      i = std::min(std::max(i, 0), side - 1);
+      idx = idx * side + i;
+    }
+    return idx;
+  }
+  void build(const Tree& t) {
+    const int dim = t.dim;
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = 1e300;
+      double hi = -1e300;
+      for (int i = 0; i < t.ns; ++i) {
+        const double c = k == 0 ? t.pts[i].x : (k == 1 ? t.pts[i].y : t.pts[i].z);
+        lo[k] = std::min(lo[k], c);
+        hi = std::max(hi, c);
+      }
+      inv[k] = hi > lo[k] ? 1.0 / (hi - lo[k]) : 1.0;
+    }
+    side = dim == 3 ? 64 : 512;
+    cell.assign(dim == 3 ? side * side * side : side * side, -1);
+    for (size_t s = 0; s < t.s.size(); ++s) {
+      if (!t.s[s].alive) continue;
+      P3 c{0, 0, 0};
+      for (int i = 0; i <= dim; ++i) {
+        c.x += t.pts[t.s[s].v[i]].x / (dim + 1);
+        c.y += t.pts[t.s[s].v[i]].y / (dim + 1);
+        c.z += t.pts[t.s[s].v[i]].z / (dim + 1);
+      }
+      cell[index(c, dim)] = (int)s;
+    }
+  }
+  int start(const Tree& t, const P3& p) const {
+    int s = cell[index(p, t.dim)];
+    if (s < 0 || !t.s[s].alive) {
+      s = t.last;
+      while (!t.s[s].alive) --s;
+    }
+    return s;
+  }
+};
+
+int nrounds_last = 0;  // rounds of the last parallel build (diagnostics)
+
+int build_parallel(Tree& t, int64_t n, int threads, int64_t prefix) {
+  const int nv = t.dim + 1;
+  std::vector<int> order;
+  for (int64_t k = 0; k < n; ++k)
+    if (t.dup_of[k] < 0) order.push_back((int)(t.ns + k));
+  const int64_t seq = std::min<int64_t>(prefix, (int64_t)order.size());
+  for (int64_t i = 0; i < seq; ++i) {
+    const int rc = insert_vertex(t, order[i]);
+    if (rc != OK) return rc;
+  }
+  const int64_t m = (int64_t)order.size() - seq;
+  if (m <= 0) return OK;
+  Grid grid;
+  grid.build(t);
+  Pool pool(threads);
+  // make_queue: conflict region and 2-ring of every remaining point
+  std::vector<std::vector<int>> ring(m);
+  std::vector<long long> nex(threads, 0);
+  std::vector<int> qstatus(m, OK);
+  pool.run(m, [&](int64_t i, int tid) {
+    Update u;
+    compute_update(t, order[seq + i], grid.start(t, t.pts[order[seq + i]]), u, &nex[tid]);
+    qstatus[i] = u.status;
+    std::vector<int>& r = ring[i];
+    for (int c : u.cav)
+      for (int f = 0; f < nv; ++f) {
+        const int a = t.s[c].n[f];
+        if (a < 0) continue;
+        for (int g = 0; g < nv; ++g)
+          if (t.s[a].n[g] >= 0) r.push_back(t.s[a].n[g]);
+      }
+    std::sort(r.begin(), r.end());
+    r.erase(std::unique(r.begin(), r.end()), r.end());
+  });
+  for (int64_t i = 0; i < m; ++i)
+    if (qstatus[i] != OK) return qstatus[i];
+  // find_placement: greedy rounds over shared 2-ring simplices
+  std::vector<int> placement(m, 1);
+  {
+    std::unordered_map<int, int64_t> last;  // simplex -> last point that holds it in its 2-ring
+    last.reserve(m * 8);
+    int maxr = 1;
+    for (int64_t i = 0; i < m; ++i) {
+      int r = 1;
+      for (int site : ring[i]) {
+        auto it = last.find(site);
+        if (it != last.end()) r = std::max(r, placement[it->second] + 1);
+      }
+      for (int site : ring[i]) last[site] = i;
+      placement[i] = r;
+      maxr = std::max(maxr, r);
+    }
+    t.maxcav = std::max<long long>(t.maxcav, 0);
+    nrounds_last = maxr;
+    std::vector<std::vector<int64_t>> rounds(maxr + 1);
+    for (int64_t i = 0; i < m; ++i) rounds[placement[i]].push_back(i);
+    ring.clear();
+    ring.shrink_to_fit();
+    std::vector<Update> ups;
+    for (int r = 1; r <= maxr; ++r) {
+      const auto& batch = rounds[r];
+      if (batch.empty()) continue;
+      ups.assign(batch.size(), Update());
+      pool.run((int64_t)batch.size(), [&](int64_t i, int tid) {
+        const int vid = order[seq + batch[i]];
+        compute_update(t, vid, grid.start(t, t.pts[vid]), ups[i], &nex[tid]);
+      });
+      for (auto& u : ups) {
+        bool fresh = u.status == OK;
+        for (int c : u.cav) fresh = fresh && t.s[c].alive;
+        for (const auto& F : u.bnd) fresh = fresh && (F.outer < 0 || t.s[F.outer].alive);
+        if (!fresh) {  // the tree changed under this update: recompute it now
+          int start = grid.start(t, t.pts[u.vid]);
+          if (!u.cav.empty() && u.cav[0] < (int)t.s.size() && t.s[u.cav[0]].alive) start = u.cav[0];
+          compute_update(t, u.vid, start, u, &t.nexact);
+          if (u.status != OK) return u.status;
+        }
+        apply_update(t, u);
+      }
+    }
+  }
+  for (long long e : nex) t.nexact += e;
+  return OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -705,49 +1099,7 @@ void* vdo_build(int dim, const double* pts, int64_t n, uint64_t seed, int* statu
     if (o < 0) std::swap(s0.v[0], s0.v[1]);
   }
   t->s.push_back(s0);
-  // duplicate groups: keep the smallest priority
-  t->dup_of.assign(n, -1);
-  {
-    struct K {
-      double x, y, z;
-      bool operator==(const K& o) const { return x == o.x && y == o.y && z == o.z; }
-    };
-    struct H {
-      size_t operator()(const K& k) const {
-        uint64_t a, b, c;
-        memcpy(&a, &k.x, 8);
-        memcpy(&b, &k.y, 8);
-        memcpy(&c, &k.z, 8);
-        return (size_t)(a * 0x9E3779B97F4A7C15ULL ^ (b + 0x632BE59BD9B4E019ULL) * 31 ^ c);
-      }
-    };
-    std::unordered_map<K, int64_t, H> best;
-    best.reserve(n * 2);
-    for (int64_t k = 0; k < n; ++k) {
-      const P3& p = t->pts[t->ns + k];
-      K key{p.x == 0.0 ? 0.0 : p.x, p.y == 0.0 ? 0.0 : p.y, p.z == 0.0 ? 0.0 : p.z};
-      auto it = best.find(key);
-      if (it == best.end()) {
-        best.emplace(key, k);
-      } else {
-        int64_t j = it->second;
-        uint32_t pk = priority((uint32_t)(t->ns + k), seed), pj = priority((uint32_t)(t->ns + j), seed);
-        if (pk < pj) {
-          t->dup_of[j] = (int)k;
-          it->second = k;
-        } else {
-          t->dup_of[k] = (int)j;
-        }
-      }
-    }
-    // resolve chains to the final kept index
-    for (int64_t k = 0; k < n; ++k) {
-      if (t->dup_of[k] < 0) continue;
-      const P3& p = t->pts[t->ns + k];
-      K key{p.x == 0.0 ? 0.0 : p.x, p.y == 0.0 ? 0.0 : p.y, p.z == 0.0 ? 0.0 : p.z};
-      t->dup_of[k] = (int)best[key];
-    }
-  }
+  mark_duplicates(*t, n, seed);
   for (int64_t k = 0; k < n; ++k) {
     if (t->dup_of[k] >= 0) continue;
     int rc = insert_vertex(*t, (int)(t->ns + k));
@@ -759,7 +1111,46 @@ void* vdo_build(int dim, const double* pts, int64_t n, uint64_t seed, int* statu
   return t;
 }
 
+// The reference's parallel path (see build_parallel) on `threads` host
+// threads; `prefix` points are inserted one at a time first (1e5 in
+// src/lib.rs:108).  Same result as vdo_build.
+void* vdo_build_parallel(int dim, const double* pts, int64_t n, uint64_t seed, int threads, int64_t prefix,
+                         int* status) {
+  Tree* t = new Tree();
+  t->dim = dim;
+  t->ns = dim + 1;
+  *status = OK;
+  if ((dim != 2 && dim != 3) || n < 1 || threads < 1) {
+    *status = ERR_ARG;
+    return t;
+  }
+  double sv[12], R;
+  super_vertices(dim, pts, n, sv, &R);
+  for (int i = 0; i <= dim; ++i) t->pts.push_back({sv[3 * i], sv[3 * i + 1], sv[3 * i + 2]});
+  for (int64_t k = 0; k < n; ++k)
+    t->pts.push_back({pts[k * dim], pts[k * dim + 1], dim == 3 ? pts[k * dim + 2] : 0.0});
+  Simplex s0;
+  s0.alive = true;
+  for (int i = 0; i < 4; ++i) {
+    s0.v[i] = i <= dim ? i : -1;
+    s0.n[i] = -1;
+  }
+  P3 q[4];
+  for (int i = 0; i <= dim; ++i) q[i] = t->pts[i];
+  const int o = exact_orient(dim, q);
+  if (o == 0) {
+    *status = ERR_DEGENERATE;
+    return t;
+  }
+  if (o < 0) std::swap(s0.v[0], s0.v[1]);
+  t->s.push_back(s0);
+  mark_duplicates(*t, n, seed);
+  *status = build_parallel(*t, n, threads, prefix);
+  return t;
+}
+
 void vdo_free(void* h) { delete (Tree*)h; }
+int vdo_parallel_rounds(void) { return nrounds_last; }
 
 int64_t vdo_num_duplicates(void* h) {
   Tree* t = (Tree*)h;

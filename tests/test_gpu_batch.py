@@ -115,3 +115,21 @@ def test_batch_errors_are_statuses(vd):
     with pytest.raises(vd.VDError):
         t = vd.DelaunayTree.create(3)
         t.add_points_to_tree(np.random.default_rng(1).random((10, 3)))  # no super simplex yet
+
+
+def test_autotuned_batch_same_result(vd):
+    torch = pytest.importorskip("torch")
+    sizes = W.c4_sizes(40, seed=W.config_seed(4) + 7)
+    sets = sets_of(sizes, 3, 1300)
+    pts = np.concatenate(sets)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    d = torch.from_numpy(pts).cuda()
+    t = vd.DelaunayTree.create(3)
+    cfg = t.autotune_batch(d.data_ptr(), off, sample_points=60_000)
+    assert 4 <= cfg["warps_per_sm"] <= 32 and cfg["passes"] in (1, 2, 3) and cfg["sample_sets"] >= 1
+    uv, eoff = t.batch(pts, off, seed=8)
+    for s, p in enumerate(sets):
+        assert np.array_equal(uv[eoff[s]:eoff[s + 1]].astype(np.int64), single(vd, p, 8))
+    ok, det = t.check_delaunay(details=True)
+    assert ok, det
+    t.close()

@@ -7,6 +7,8 @@ import os
 import numpy as np
 import pytest
 
+from voronoids_gb300 import workloads as W
+
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
@@ -151,3 +153,14 @@ def test_priority_is_a_bijective_mix(oracle):
     # the GPU uses the same mix; spot-check distinctness over a window
     vals = {oracle.priority(v, 12345) for v in range(20000)}
     assert len(vals) == 20000
+
+
+@pytest.mark.parametrize("dim,n,prefix", [(3, 6000, 1000), (2, 8000, 500), (3, 3000, 10_000)])
+def test_parallel_reference_path_same_triangulation(oracle, dim, n, prefix):
+    # the reference's parallel path (queue, greedy rounds, per-round updates)
+    # restated on threads: the same unique triangulation as the sequential one
+    p = W.uniform_points(n, dim, 404 + n)
+    a = oracle.Triangulation(p, seed=3)
+    b = oracle.Triangulation(p, seed=3, threads=4, prefix=prefix)
+    assert a.status == 0 and b.status == 0
+    assert np.array_equal(a.edges(), b.edges())

@@ -190,14 +190,20 @@ struct vd_tree {
   // highest simplex slot handed out since the last reset: slots below it
   // may hold simplices of an earlier build and are cleared on reset
   int64_t simp_hwm = 0;
+  // launch shape: blocks of 256 threads per SM for point-per-thread kernels,
+  // warps per SM for candidate-per-warp kernels (see vd_autotune_batch)
+  int blocks_per_sm = 8;
+  int warps_per_sm = 20;
 };
 
 namespace {
 
+constexpr int kMaxWarpsPerSm = 32;
+
 vd::Launch launch_of(const vd_tree* t) {
   vd::Launch L;
-  L.blocks = t->sms * 8;
-  L.warps = t->sms * 5 * 4;
+  L.blocks = t->sms * t->blocks_per_sm;
+  L.warps = t->sms * t->warps_per_sm;
   L.stream = t->stream;
   return L;
 }
@@ -463,7 +469,7 @@ int alloc_tree(vd_tree* t, int dim, void* stream) {
       dalloc(&t->T.lev_off, vd::kMaxLevels + 1))
     return vd::E_NOMEM;
   if (cudaMallocHost((void**)&t->h_mm, 8 * sizeof(unsigned long long)) != cudaSuccess) return vd::E_NOMEM;
-  t->T.cap_wchunk = t->sms * 20;
+  t->T.cap_wchunk = t->sms * kMaxWarpsPerSm;
   if (dalloc(&t->T.wchunk, t->T.cap_wchunk)) return vd::E_NOMEM;
   t->ncells = vd::hint_cells(dim, single_hint_levels(dim));
   if (dalloc(&t->T.hint, t->ncells)) return vd::E_NOMEM;
@@ -1485,6 +1491,125 @@ int vd_num_sets(vd_tree* t, int* nsets) {
   if (ready(t) || !nsets) return VD_ERR_ARG;
   *nsets = t->nsets;
   return VD_OK;
+}
+
+int vd_set_launch(vd_tree* t, int warps_per_sm, int blocks_per_sm) {
+  if (ready(t) || warps_per_sm < 4 || warps_per_sm > kMaxWarpsPerSm || (warps_per_sm & 3) || blocks_per_sm < 1 ||
+      blocks_per_sm > 32)
+    return VD_ERR_ARG;
+  t->warps_per_sm = warps_per_sm;
+  t->blocks_per_sm = blocks_per_sm;
+  return VD_OK;
+}
+
+int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, int nsets, int64_t sample_points,
+                      int64_t* out) {
+  if (ready(t) || !d_pts || !offsets || nsets < 1 || offsets[0] != 0) return VD_ERR_ARG;
+  for (int s = 0; s < nsets; ++s)
+    if (offsets[s + 1] <= offsets[s]) return VD_ERR_ARG;
+  const int dim = t->dim;
+  // sample: every stride-th set (the size mix of the batch), up to sample_points
+  const int64_t total = offsets[nsets];
+  const int64_t want = std::max<int64_t>(1, std::min(sample_points, total));
+  const int stride = (int)std::max<int64_t>(1, total / want);
+  std::vector<int64_t> soff(1, 0);
+  std::vector<int> pick;
+  for (int s = 0; s < nsets && soff.back() < want; s += stride) {
+    pick.push_back(s);
+    soff.push_back(soff.back() + offsets[s + 1] - offsets[s]);
+  }
+  const int ns = (int)pick.size();
+  const int64_t npts = soff.back();
+  double* d_sample = nullptr;
+  uint2* d_uv = nullptr;
+  const int64_t cap = (dim == 3 ? 10 : 4) * npts + 64;
+  if (dalloc(&d_sample, (size_t)(npts * dim)) || dalloc(&d_uv, (size_t)cap)) {
+    dfree(d_sample);
+    return VD_ERR_NOMEM;
+  }
+  for (int i = 0; i < ns; ++i)
+    cudaMemcpyAsync(d_sample + soff[i] * dim, d_pts + offsets[pick[i]] * dim,
+                    sizeof(double) * (offsets[pick[i] + 1] - offsets[pick[i]]) * dim, cudaMemcpyDeviceToDevice,
+                    t->stream);
+  struct Cfg {
+    int wps, bps, passes, thin;
+    double ratio;
+  };
+  std::vector<int64_t> eoff(ns + 1);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int rc = VD_OK;
+  auto apply = [&](const Cfg& c) {
+    t->warps_per_sm = c.wps;
+    t->blocks_per_sm = c.bps;
+    t->tuning.passes = c.passes;
+    t->tuning.thin = c.thin;
+    t->ratio = c.ratio;
+  };
+  auto time_cfg = [&](const Cfg& c) -> double {
+    apply(c);
+    double best = 1e30;
+    for (int rep = 0; rep < 2 && !rc; ++rep) {
+      cudaEventRecord(e0, t->stream);
+      int r = batch_reset_device(t, d_sample, soff.data(), ns);
+      if (!r) r = insert_device(t, d_sample, npts, 0x5eedULL);  // one seed: the second run replays graphs
+      if (r == VD_ERR_DUPLICATE) r = VD_OK;
+      if (!r) r = batch_edges(t, d_uv, cap, eoff.data(), nullptr);
+      cudaEventRecord(e1, t->stream);
+      if (r) {
+        rc = r;
+        break;
+      }
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best = std::min(best, (double)ms);
+    }
+    return best;
+  };
+  Cfg best{t->warps_per_sm, t->blocks_per_sm, t->tuning.passes, t->tuning.thin, t->ratio};
+  double best_ms = time_cfg(best);
+  // coordinate descent, one sweep per coordinate
+  const int wps_c[] = {8, 12, 16, 20, 24, 28, 32};
+  const int bps_c[] = {4, 8, 16};
+  const int pass_c[] = {1, 2, 3};
+  const int thin_c[] = {1, 2};
+  const double ratio_c[] = {0.06, 0.12, 0.25, 0.5};
+  auto sweep = [&](auto field, const auto& values) {
+    for (const auto& v : values) {
+      if (rc) return;
+      Cfg c = best;
+      field(c, v);
+      const double ms = time_cfg(c);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
+    }
+  };
+  sweep([](Cfg& c, double v) { c.ratio = v; }, ratio_c);
+  sweep([](Cfg& c, int v) { c.passes = v; }, pass_c);
+  sweep([](Cfg& c, int v) { c.thin = v; }, thin_c);
+  sweep([](Cfg& c, int v) { c.wps = v; }, wps_c);
+  sweep([](Cfg& c, int v) { c.bps = v; }, bps_c);
+  apply(best);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamSynchronize(t->stream);
+  dfree(d_sample);
+  dfree(d_uv);
+  if (out) {
+    out[0] = best.wps;
+    out[1] = best.bps;
+    out[2] = best.passes;
+    out[3] = best.thin;
+    out[4] = (int64_t)(best.ratio * 1000.0 + 0.5);
+    out[5] = (int64_t)(best_ms * 1000.0);
+    out[6] = npts;
+    out[7] = ns;
+  }
+  return rc;
 }
 
 int vd_locate(vd_tree* t, const double* p, int64_t* out, int64_t cap, int64_t* n) {

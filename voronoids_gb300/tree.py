@@ -128,6 +128,22 @@ class DelaunayTree:
             _check(rc, "batch_device")
         return eoff
 
+    def set_launch(self, warps_per_sm=20, blocks_per_sm=8):
+        _check(_native.load().vd_set_launch(self._h, int(warps_per_sm), int(blocks_per_sm)), "set_launch")
+
+    def autotune_batch(self, ptr, offsets, sample_points=2_000_000):
+        """Tune launch shape and round settings on a sample of a device batch;
+        returns the chosen setting."""
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        out = np.zeros(8, dtype=np.int64)
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        _check(_native.load().vd_autotune_batch(self._h, ctypes.c_void_p(ptr), off.ctypes.data_as(i64p),
+                                                 off.shape[0] - 1, int(sample_points), out.ctypes.data_as(i64p)),
+               "autotune_batch")
+        keys = ("warps_per_sm", "blocks_per_sm", "passes", "thin", "ratio_x1000", "sample_us", "sample_points",
+                "sample_sets")
+        return dict(zip(keys, out.tolist()))
+
     def num_sets(self):
         n = ctypes.c_int(0)
         _check(_native.load().vd_num_sets(self._h, ctypes.byref(n)), "num_sets")
