@@ -56,9 +56,10 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_POINTS)
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", default="c2", choices=["c2", "c4", "c5"],
-                   help="c2: 1M-point 3D build (the headline line); c4: 4,096 sets batched vs one set per "
-                        "launch; c5: Poisson request stream through the serving loop")
+    p.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
+                   help="c2: 1M-point 3D build (the headline line); c3: near-degenerate 262,144 points with "
+                        "predicate fallback rates; c4: 4,096 sets batched vs one set per launch; c5: Poisson "
+                        "request stream through the serving loop")
     p.add_argument("--requests", type=int, default=20_000, help="c5: requests in the stream")
     p.add_argument("--slots", type=int, default=3, help="c5: server slots")
     p.add_argument("--max-batch-points", type=int, default=2_000_000, help="c5: largest batch a slot forms")
@@ -76,7 +77,7 @@ def measured_peaks():
 
 def profile_traffic(kernel):
     """dram bytes per launch of `kernel` from the committed ncu summary, or None."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_c2.md")
+    path = os.path.join(ROOT, "profiles", f"{kernel}_c2_1m.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -190,6 +191,75 @@ def run_reference(args, rank):
         "cpu_baseline": {"value": round(v, 4), "unit": "Mpts/s", "cores": threads, "kind": "port",
                          "sample": cpu_sample_desc(threads)},
         "e2e": {"value": round(v, 4), "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_c3(args):
+    """Near-degenerate 3D build (jittered lattice + tight Gaussian clusters):
+    time, exactness and the share of predicates each precision tier decided."""
+    import torch
+    from voronoids_gb300 import _native
+    from voronoids_gb300 import workloads as W
+    L = _native.load()
+    pts_h = W.c3_points()
+    n = len(pts_h)
+    pts_d = torch.from_numpy(pts_h).cuda()
+    cap = 10 * n + 1024
+    uv_d = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    st = ctypes.c_int(0)
+    tree = ctypes.c_void_p(L.vd_tree_new_device(3, ctypes.c_void_p(pts_d.data_ptr()), n,
+                                                ctypes.c_void_p(stream.cuda_stream), ctypes.byref(st)))
+    m = ctypes.c_int64(0)
+
+    def step():
+        rc = L.vd_delaunay_device(tree, ctypes.c_void_p(pts_d.data_ptr()), n, SEED, ctypes.c_void_p(uv_d.data_ptr()),
+                                  cap, ctypes.byref(m))
+        if rc not in (0, 4):
+            raise SystemExit(f"vd_delaunay_device failed: {rc}")
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    times = []
+    clk = Clocks(0)
+    clk.start()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clocks = clk.stop()
+    s1 = _native.VdStats()
+    L.vd_get_stats(tree, ctypes.byref(s1))
+    stats = {k: getattr(s1, k) for k, _ in s1._fields_}
+    ok = ctypes.c_int(0)
+    viol = np.zeros(6, dtype=np.int64)
+    L.vd_check_delaunay(tree, ctypes.byref(ok), viol.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    L.vd_tree_free(tree)
+    tot = stats["pred_f32"] + stats["pred_f64"] + stats["pred_exact"]
+    ms = float(np.mean(times))
+    line = {
+        "metric": "Mpts/s 3D near-degenerate build; predicate tier shares", "value": round(n / (ms / 1e3) / 1e6, 4),
+        "unit": "Mpts/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "262,144 3D points: 131,072 distinct sites of the 64^3 lattice (i/64) with uniform "
+                               "jitter +-1e-12 per coordinate, 131,072 from 64 Gaussians (centres uniform in the "
+                               "cube, sigma 0.01, not clipped); splitmix64 seed 0xD1A00003", "points": n,
+                   "l2": "flushed between steps (256 MB write)"},
+        "predicates": {"decided_f32_filter": stats["pred_f32"], "decided_f64_filter": stats["pred_f64"],
+                       "decided_exact": stats["pred_exact"], "of_exact_by_perturbation": stats["pred_sos"],
+                       "fallback_rate_f32_to_f64": round((stats["pred_f64"] + stats["pred_exact"]) / max(tot, 1), 6),
+                       "fallback_rate_f64_to_exact": round(stats["pred_exact"] /
+                                                           max(stats["pred_f64"] + stats["pred_exact"], 1), 6)},
+        "validator_ok": bool(ok.value), "violations": viol.tolist(), "edges": int(m.value),
+        "build_stats": {k: stats[k] for k in ("rounds", "max_cavity", "max_facets", "spilled", "cavity_tests")},
+        "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
 
@@ -412,6 +482,9 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank)
         return
+    if args.workload == "c3":
+        run_c3(args)
+        return
     if args.workload == "c4":
         run_c4(args)
         return
@@ -552,6 +625,13 @@ def main():
                "h2d_bytes_per_step": int(n * 3 * 8), "d2h_bytes_per_step": int(m.value * 8),
                "ms_per_step": round(ems, 3)}
 
+    # whole build against HBM: algorithmic bytes per inserted 3D point
+    # 1820 + 128 ln N (point, killed and created simplex records, outer
+    # neighbour rewrites, edge output, relocations)
+    bpp = 1820.0 + 128.0 * math.log(n)
+    peak_b, _ = measured_peaks()
+    build_roof = {"bytes_per_point": round(bpp, 1), "achieved": round(bpp * n / (ms / 1e3) / 1e9, 2),
+                  "peak": peak_b, "unit": "GB/s", "frac": round(bpp * n / (ms / 1e3) / 1e9 / peak_b, 5)}
     cpu = cpu_baseline() if rank == 0 and world == 1 else None
     edges = int(m.value)
     L.vd_tree_free(tree)
@@ -571,6 +651,7 @@ def main():
             "build_stats": {k: stats[k] for k in ("rounds", "inserted", "max_cavity", "pred_f32", "pred_f64",
                                                   "pred_exact", "walk_steps", "cavity_tests", "searched")},
             "kernel_share": kernel_share,
+            "build_roofline": build_roof,
             "ms_per_step_profiled": round(float(np.mean(ptimes)), 3),
         }
         print(json.dumps(line), flush=True)

@@ -110,6 +110,12 @@ int vd_insert_point(vd_tree* t, const double* p);
  * ids of the simplices whose circumsphere strictly contains `p` (perturbed),
  * sorted ascending.  *n receives the count even when it exceeds `cap`. */
 int vd_locate(vd_tree* t, const double* p, int64_t* out, int64_t cap, int64_t* n);
+/* The same for nq query points at once (host arrays): the conflict region of
+ * query i is ids[offsets[i] .. offsets[i+1]) (offsets: nq + 1 entries),
+ * numbered as vd_simplices exports the simplices, each list sorted.  With
+ * `ids` NULL only the offsets are filled.  VD_ERR_OUTSIDE if a query lies
+ * outside the super simplex (its list is empty).  Single-set trees. */
+int vd_locate_points(vd_tree* t, const double* pts, int64_t nq, int64_t* offsets, int64_t* ids, int64_t cap);
 
 /* Vertices inserted so far (super vertices excluded). */
 int vd_num_vertices(vd_tree* t, int64_t* n);

@@ -1612,13 +1612,86 @@ int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, i
   return rc;
 }
 
+int vd_locate_points(vd_tree* t, const double* pts, int64_t nq, int64_t* offsets, int64_t* ids, int64_t cap) {
+  if (ready(t) || !t->has_geometry || t->nsets != 1 || nq < 0 || (nq > 0 && !pts) || !offsets) return VD_ERR_ARG;
+  offsets[0] = 0;
+  if (nq == 0) return VD_OK;
+  int rc = sync_counters(t);
+  if (rc) return rc;
+  const int dim = t->dim;
+  const int nsimp = t->hctr->nsimp;
+  const vd::Launch L = launch_of(t);
+  int *flags = nullptr, *rank = nullptr, *tmp = nullptr, *out = nullptr, *cnt = nullptr;
+  double* dq = nullptr;
+  const int64_t chunk = std::min<int64_t>(nq, 1 << 16);
+  int cap_per = 256;
+  if (dalloc(&flags, nsimp + 1) || dalloc(&rank, nsimp + 1) || dalloc(&tmp, vd::scan_scratch_ints(nsimp + 1)) ||
+      dalloc(&dq, (size_t)(chunk * dim)) || dalloc(&cnt, chunk) || dalloc(&out, (size_t)(chunk * cap_per))) {
+    rc = vd::E_NOMEM;
+  }
+  if (!rc) vd::launch_live_rank(t->T, L, nsimp, flags, rank, tmp);
+  std::vector<int> hc(chunk), ho;
+  bool outside = false;
+  int64_t total = 0;
+  for (int64_t q0 = 0; q0 < nq && !rc; q0 += chunk) {
+    const int m = (int)std::min<int64_t>(chunk, nq - q0);
+    cudaMemcpyAsync(dq, pts + q0 * dim, sizeof(double) * m * dim, cudaMemcpyHostToDevice, t->stream);
+    vd::launch_locate(t->T, L, dim, dq, m, cap_per, rank, out, cnt);
+    cudaMemcpyAsync(hc.data(), cnt, sizeof(int) * m, cudaMemcpyDeviceToHost, t->stream);
+    if (cudaStreamSynchronize(t->stream) != cudaSuccess) {
+      rc = vd::E_CUDA;
+      break;
+    }
+    int need = 0;
+    for (int i = 0; i < m; ++i) need = std::max(need, hc[i]);
+    if (need > cap_per) {  // a region larger than the per-query room: rerun this chunk with enough
+      cap_per = need;
+      dfree(out);
+      if (dalloc(&out, (size_t)m * cap_per)) {
+        rc = vd::E_NOMEM;
+        break;
+      }
+      vd::launch_locate(t->T, L, dim, dq, m, cap_per, rank, out, cnt);
+      cudaMemcpyAsync(hc.data(), cnt, sizeof(int) * m, cudaMemcpyDeviceToHost, t->stream);
+    }
+    ho.resize((size_t)m * cap_per);
+    cudaMemcpyAsync(ho.data(), out, sizeof(int) * ho.size(), cudaMemcpyDeviceToHost, t->stream);
+    if (cudaStreamSynchronize(t->stream) != cudaSuccess) {
+      rc = vd::E_CUDA;
+      break;
+    }
+    for (int i = 0; i < m; ++i) {
+      const int c = std::max(hc[i], 0);
+      outside = outside || hc[i] < 0;
+      offsets[q0 + i + 1] = offsets[q0 + i] + c;
+      if (ids && total + c <= cap) {
+        int64_t* dst = ids + total;
+        for (int k = 0; k < c; ++k) dst[k] = ho[(size_t)i * cap_per + k];
+        std::sort(dst, dst + c);
+      }
+      total += c;
+    }
+  }
+  dfree(flags);
+  dfree(rank);
+  dfree(tmp);
+  dfree(dq);
+  dfree(cnt);
+  dfree(out);
+  if (rc) return rc;
+  if (t->hctr->err) return t->hctr->err;
+  if (ids && total > cap) return VD_ERR_ARG;
+  return outside ? VD_ERR_OUTSIDE : VD_OK;
+}
+
 int vd_locate(vd_tree* t, const double* p, int64_t* out, int64_t cap, int64_t* n) {
-  (void)t;
-  (void)p;
-  (void)out;
-  (void)cap;
-  (void)n;
-  return VD_ERR_ARG;  // implemented in a later revision of the query API
+  if (!n) return VD_ERR_ARG;
+  int64_t off[2] = {0, 0};
+  int rc = vd_locate_points(t, p, 1, off, nullptr, 0);
+  *n = off[1];
+  if (rc || !out) return rc;
+  if (cap < off[1]) return VD_ERR_ARG;
+  return vd_locate_points(t, p, 1, off, out, cap);
 }
 
 }  // extern "C"

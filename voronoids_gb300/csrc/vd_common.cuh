@@ -254,6 +254,16 @@ struct EdgeScratch {
   int64_t cap_buf;
 };
 int64_t scan_scratch_ints(int64_t n);
+// out[i] = sum(in[0..i)) for i < n, out[n] = total; tmp: scan_scratch_ints(n).
+void scan_ints(const int* in, int* out, int64_t n, int* tmp, cudaStream_t st);
+// Conflict regions of nq query points (vd_locate.cu): slots of query i in
+// out[i * cap_per ..] numbered by rank[], count in counts[i] (-1: outside
+// the super simplex; above cap_per: truncated).  rank[s] = position of live
+// slot s among the
+// live slots (nsimp + 1 entries, tmp: scan_scratch_ints(nsimp)).
+void launch_locate(const DevTree& T, const Launch& L, int dim, const double* d_q, int nq, int cap_per,
+                   const int* rank, int* out, int* counts);
+void launch_live_rank(const DevTree& T, const Launch& L, int nsimp, int* flags, int* rank, int* tmp);
 void launch_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_in,
                   const EdgeScratch& S, uint2* d_out);
 

@@ -256,6 +256,8 @@ int64_t scan_scratch_ints(int64_t n) {
 }
 
 // Returns the number of unique edges written to d_out (or -1 on a CUDA error).
+void scan_ints(const int* in, int* out, int64_t n, int* tmp, cudaStream_t st) { exclusive_scan(in, out, n, tmp, st); }
+
 int64_t run_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_in,
                   const EdgeScratch& S, uint2* d_out, int64_t cap_out, int* d_total_pair, int* h_total_pair) {
   cudaStream_t st = L.stream;

@@ -144,6 +144,28 @@ class DelaunayTree:
                 "sample_sets")
         return dict(zip(keys, out.tolist()))
 
+    def locate(self, points):
+        """Conflict regions (``locate``): for each query point the sorted ids
+        (numbered as :meth:`simplices` returns them) of the simplices whose
+        circumsphere strictly contains it.  One point -> one array; many ->
+        a list of arrays."""
+        q = np.asarray(points, dtype=np.float64)
+        single = q.ndim == 1
+        q = _points(q.reshape(1, -1) if single else q, self.dim)
+        nq = q.shape[0]
+        off = np.zeros(nq + 1, dtype=np.int64)
+        L = _native.load()
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        rc = L.vd_locate_points(self._h, _dp(q), nq, off.ctypes.data_as(i64p), None, 0)
+        if rc not in (_native.VD_OK, 6):
+            _check(rc, "locate")
+        ids = np.zeros(max(int(off[-1]), 1), dtype=np.int64)
+        rc = L.vd_locate_points(self._h, _dp(q), nq, off.ctypes.data_as(i64p), ids.ctypes.data_as(i64p), ids.shape[0])
+        if rc not in (_native.VD_OK, 6):
+            _check(rc, "locate")
+        out = [ids[off[i]:off[i + 1]] for i in range(nq)]
+        return out[0] if single else out
+
     def num_sets(self):
         n = ctypes.c_int(0)
         _check(_native.load().vd_num_sets(self._h, ctypes.byref(n)), "num_sets")
