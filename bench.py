@@ -285,13 +285,13 @@ def run_c4(args):
     offp = off.astype(np.int64)
 
     # autotune launch shape and round settings on a 2M-point sample of the sets
-    tuned = np.zeros(8, dtype=np.int64)
+    tuned = np.zeros(9, dtype=np.int64)
     rc = L.vd_autotune_batch(tree, ctypes.c_void_p(pts_d.data_ptr()), offp.ctypes.data_as(i64p), nsets, 2_000_000,
                              tuned.ctypes.data_as(i64p))
     if rc not in (0, 4):
         raise SystemExit(f"vd_autotune_batch failed: {rc}")
     tuned = dict(zip(("warps_per_sm", "blocks_per_sm", "passes", "thin", "ratio_x1000", "sample_us",
-                      "sample_points", "sample_sets"), tuned.tolist()))
+                      "sample_points", "sample_sets", "adjacent"), tuned.tolist()))
 
     def batched():
         rc = L.vd_batch_delaunay_device(tree, ctypes.c_void_p(pts_d.data_ptr()), offp.ctypes.data_as(i64p), nsets,
@@ -645,7 +645,8 @@ def main():
                                    "input-index edge list", "points": n,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "flushed between steps (256 MB write)", "edges": edges,
-                       "tuning": "3D defaults: 2 resolution passes, thinning radius 2, priority levels 64 x1.25 fed at 0.12 x inserted, rounds replayed as CUDA graphs"},
+                       "tuning": "3D defaults: adjacent round mode, 2 resolution passes, thinning radius 2, "
+                                 "priority levels 64 x1.25 fed at 0.12 x inserted, rounds replayed as CUDA graphs"},
             "clocks": clocks, "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
             "cpu_baseline": cpu,
             "build_stats": {k: stats[k] for k in ("rounds", "inserted", "max_cavity", "pred_f32", "pred_f64",

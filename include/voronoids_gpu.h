@@ -171,8 +171,15 @@ int vd_set_profiling(vd_tree* t, int on);
 int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth, double ratio);
 /* Round tuning: resolution passes per round (1..6) and the thinning radius
  * (1 = a nominee must hold its simplex and face neighbours, 2 = and no lower
- * nominee two faces away).  Defaults: 3D 2 passes / radius 2, 2D 3 / 1. */
+ * nominee two faces away).  Defaults: 3D 2 passes / radius 2, 2D 2 / 1. */
 int vd_set_tuning(vd_tree* t, int passes, int thin);
+/* Round mode (no reference counterpart).  0: winners of a pass have
+ * disjoint cavities and no cavity touches another's outer shell, the
+ * reference's 2-ring independence (src/scheduler.rs:30-55).  1 (default):
+ * cavities only need to be disjoint; a cavity next to a lower-priority cavity
+ * wins if the shared facets stay locally Delaunay (exact test), and the two
+ * stars are stitched after the pass.  Same triangulation either way. */
+int vd_set_adjacent(vd_tree* t, int on);
 /* Rounds are launched in chunks captured once as CUDA graphs and replayed
  * (default on; profiling and tracing launch kernel by kernel).  No reference
  * counterpart. */
@@ -219,12 +226,13 @@ int vd_batch_delaunay_device(vd_tree* t, const double* d_pts, const int64_t* off
 int vd_set_launch(vd_tree* t, int warps_per_sm, int blocks_per_sm);
 /* Autotuner for batched builds (no reference counterpart).  Times batched
  * builds of a sample of the sets (every k-th set, about `sample_points`
- * points: the batch's size mix) with CUDA events, sweeping in turn the feed
- * ratio, resolution passes, thinning radius, warps per SM and blocks per SM,
- * and keeps the fastest setting on the tree.  out (NULL or 8 entries): warps
+ * points: the batch's size mix) with CUDA events, sweeping in turn the round
+ * mode, feed ratio, resolution passes, thinning radius, warps per SM and
+ * blocks per SM,
+ * and keeps the fastest setting on the tree.  out (NULL or 9 entries): warps
  * per SM, blocks per SM, passes, thinning radius, ratio x 1000, best sample
- * microseconds, sample points, sample sets.  The tree is left reset to the
- * sample. */
+ * microseconds, sample points, sample sets, round mode.  The tree is left
+ * reset to the sample. */
 int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, int nsets, int64_t sample_points,
                       int64_t* out);
 /* Point sets of the tree (1 unless built by vd_batch_*). */

@@ -1149,6 +1149,92 @@ void* vdo_build_parallel(int dim, const double* pts, int64_t n, uint64_t seed, i
   return t;
 }
 
+// Diagnostics: winners of one resolution pass for the next `nact` points (by
+// priority) against the tree built from the first `n_built` points, under
+// the strict rule (cavities disjoint from other cavities and their outer
+// shells) and under the relaxed rule (cavities disjoint; a cavity next to a
+// lower-priority cavity wins only if the shared facets stay locally Delaunay).
+// out: strict winners, relaxed winners, adjacent pairs, failed facet tests.
+void vdo_round_sim(int dim, const double* pts, int64_t n_built, int64_t nact, uint64_t seed, int64_t* out) {
+  Tree t;
+  t.dim = dim;
+  t.ns = dim + 1;
+  const int64_t n = n_built + nact;
+  double sv[12], R;
+  super_vertices(dim, pts, n, sv, &R);
+  for (int i = 0; i <= dim; ++i) t.pts.push_back({sv[3 * i], sv[3 * i + 1], sv[3 * i + 2]});
+  for (int64_t k = 0; k < n; ++k) t.pts.push_back({pts[k * dim], pts[k * dim + 1], dim == 3 ? pts[k * dim + 2] : 0.0});
+  Simplex s0;
+  s0.alive = true;
+  for (int i = 0; i < 4; ++i) {
+    s0.v[i] = i <= dim ? i : -1;
+    s0.n[i] = -1;
+  }
+  P3 q[4];
+  for (int i = 0; i <= dim; ++i) q[i] = t.pts[i];
+  if (exact_orient(dim, q) < 0) std::swap(s0.v[0], s0.v[1]);
+  t.s.push_back(s0);
+  for (int64_t k = 0; k < n_built; ++k) insert_vertex(t, (int)(t.ns + k));
+  const int nv = dim + 1;
+  std::vector<Update> up(nact);
+  std::vector<uint32_t> key(nact);
+  for (int64_t i = 0; i < nact; ++i) {
+    const int vid = (int)(t.ns + n_built + i);
+    int start = t.last;
+    while (!t.s[start].alive) --start;
+    compute_update(t, vid, start, up[i], &t.nexact);
+    key[i] = priority((uint32_t)vid, seed);
+  }
+  const uint32_t NONE = 0xffffffffu;
+  std::vector<uint32_t> cc(t.s.size(), NONE), cn(t.s.size(), NONE);
+  std::vector<int64_t> owner(t.s.size(), -1);
+  for (int64_t i = 0; i < nact; ++i) {
+    for (int c : up[i].cav)
+      if (key[i] < cc[c]) {
+        cc[c] = key[i];
+        owner[c] = i;
+      }
+    for (const auto& F : up[i].bnd)
+      if (F.outer >= 0) cn[F.outer] = std::min(cn[F.outer], key[i]);
+  }
+  int64_t strict = 0, relaxed = 0, adjacent = 0, failed = 0;
+  long long nsos = 0;
+  for (int64_t i = 0; i < nact; ++i) {
+    bool own = true;
+    for (int c : up[i].cav) own = own && cc[c] == key[i];
+    bool s_ok = own;
+    for (int c : up[i].cav) s_ok = s_ok && cn[c] > key[i];
+    for (const auto& F : up[i].bnd)
+      if (F.outer >= 0) s_ok = s_ok && cc[F.outer] > key[i];
+    strict += s_ok;
+    bool r_ok = own;
+    for (const auto& F : up[i].bnd) {
+      if (!r_ok) break;
+      if (F.outer < 0 || cc[F.outer] >= key[i]) continue;
+      ++adjacent;
+      // new simplex of i on this facet; the lower candidate's point must not conflict
+      P3 p[4];
+      int kk[4];
+      for (int j = 0; j < nv; ++j) {
+        kk[j] = t.s[F.simp].v[j];
+        p[j] = t.pts[kk[j]];
+      }
+      kk[F.face] = up[i].vid;
+      p[F.face] = t.pts[up[i].vid];
+      const int x = up[owner[F.outer]].vid;
+      if (insphere_sos(dim, p, kk, t.pts[x], x, &t.nexact, &nsos) > 0) {
+        ++failed;
+        r_ok = false;
+      }
+    }
+    relaxed += r_ok;
+  }
+  out[0] = strict;
+  out[1] = relaxed;
+  out[2] = adjacent;
+  out[3] = failed;
+}
+
 void vdo_free(void* h) { delete (Tree*)h; }
 int vdo_parallel_rounds(void) { return nrounds_last; }
 

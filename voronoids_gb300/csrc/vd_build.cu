@@ -400,6 +400,8 @@ __global__ void k_pick(DevTree T) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     T.ctr->nact[par ^ 1] = 0;
     for (int k = 0; k < kStages; ++k) T.ctr->nwl[k] = 0;
+    T.ctr->nwin = 0;
+    T.ctr->win_lo = 0;
   }
   const int n = T.ctr->nact[par];
   const unsigned long long ep = epoch(round);
@@ -643,10 +645,12 @@ struct WarpCav {
 };
 
 // Claims of a candidate for one resolution pass: its cavity in claim_c, every
-// outer neighbour in claim_n.  P = cavity ids, F = facet records.
+// outer neighbour in claim_n (not in adjacent mode, where cavities may touch).
+// P = cavity ids, F = facet records.
 __device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int ncav, const int* F,
-                                             int nfac, unsigned long long key, int lane) {
+                                             int nfac, unsigned long long key, int lane, int adjacent) {
   for (int i = lane; i < ncav; i += 32) atomicMin(T.claim_c + P[i], key);
+  if (adjacent) return;
   for (int j = lane; j < nfac; j += 32) {
     const int o = F[6 * j + 4];
     if (o >= 0 && !bad_simp(T, o >> 2)) atomicMin(T.claim_n + (o >> 2), key);
@@ -654,7 +658,7 @@ __device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int
 }
 
 template <int D>
-__global__ void __launch_bounds__(128) k_cavity(DevTree T) {
+__global__ void __launch_bounds__(128) k_cavity(DevTree T, int adjacent) {
   const int round = T.ctr->round;
   constexpr int MAXC = Cap<D>::MAXC, MAXF = Cap<D>::MAXF, HS = Cap<D>::HS;
   __shared__ WarpCav<D> smem[4];
@@ -714,7 +718,7 @@ __global__ void __launch_bounds__(128) k_cavity(DevTree T) {
       ncav = W.ctl.ncav;
       nfac = W.ctl.nfac;
       // the facets stay at P + kOffF; cinfo.y carries the flag (see below)
-      claim_region(T, P, ncav, P + kOffF, nfac, key, lane);
+      claim_region(T, P, ncav, P + kOffF, nfac, key, lane, adjacent);
       if (lane == 0) T.cinfo[c] = make_int4(ncav, nfac | (1 << 30), off, ST_OK);
       mcav = max(mcav, ncav);
       mfac = max(mfac, nfac);
@@ -744,7 +748,7 @@ __global__ void __launch_bounds__(128) k_cavity(DevTree T) {
     for (int i = lane; i < ncav; i += 32) P[i] = W.cav[i];
     int* F = P + ncav;
     for (int x = lane; x < 6 * nfac; x += 32) F[x] = W.fr[x];
-    claim_region(T, W.cav, ncav, W.fr, nfac, key, lane);
+    claim_region(T, W.cav, ncav, W.fr, nfac, key, lane, adjacent);
     if (lane == 0) T.cinfo[c] = make_int4(ncav, nfac, off, ST_OK);
     mcav = max(mcav, ncav);
     mfac = max(mfac, nfac);
@@ -803,12 +807,14 @@ __device__ __forceinline__ void ridge_of(const int* r, int g, int qf, int& r0, i
   }
 }
 
-// Writes one new simplex and repoints its outer neighbour.
+// Writes one new simplex and repoints its outer neighbour.  An outer
+// neighbour that another winner of this round removed (adjacent mode) is left
+// alone: the two new simplices on that facet are linked by k_fix_links.
 __device__ __forceinline__ void emit_simplex(const DevTree& T, const int* r, int myid, int4 nn, int round) {
   const int4 v = make_int4(r[0], r[1], r[2], r[3]);
   const int qf = r[5] & 3, o = r[4];
   store_simplex(T, myid, v, nn);
-  if (o >= 0 && !bad_simp(T, o >> 2)) {
+  if (o >= 0 && !bad_simp(T, o >> 2) && T.killed[o >> 2].x != round) {
     reinterpret_cast<int*>(T.simp + (o >> 2))[4 + (o & 3)] = (myid << 2) | qf;
     T.touched[o >> 2] = round;
   }
@@ -968,82 +974,134 @@ __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, i
 // Slots: the new simplex built on a boundary facet of cavity simplex k reuses
 // the slot of k when it is the first facet of k, so a point that was inside
 // k usually finds itself in (or next to) the simplex now in k's slot.
-template <int D>
-__global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last) {
+//
+// Adjacent mode (MODE 1 + 2) relaxes independence to disjoint cavities.  A
+// candidate whose boundary facet touches the cavity of a lower candidate X
+// (claim_c of the outer simplex holds X's key; X is recovered from its
+// priority) wins only if X's point is outside the new simplex it would build
+// on that facet: then the two new simplices on the facet are locally
+// Delaunay and inserting both equals inserting them one after the other.
+// MODE 1 decides (claims, facet tests, fresh slots, kill marks) for all
+// candidates of the pass, so that MODE 2, which writes the stars, knows every
+// simplex removed in the pass and leaves links into them to k_fix_links.
+template <int D, int MODE>
+__global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last, unsigned long long seed) {
+  constexpr int NV = D + 1;
   const int round = T.ctr->round;
   const int sin = 2 * pass, sout = 2 * pass + 1;
   constexpr int MAXF = Cap<D>::MAXF, MAXC = Cap<D>::MAXC;
   extern __shared__ __align__(16) unsigned char dsm[];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   WarpCommit<D>& W = reinterpret_cast<WarpCommit<D>*>(dsm)[wib];
-  const int nc = min(T.ctr->ncand, T.cap_cand);
   const unsigned long long pe = pass_epoch(round, pass);
   const int par = round & 1;
   unsigned long long nwon = 0, ncreated = 0, nkilled = 0;
   int nholes = 0;
+  vdp::Tally tl = {0, 0, 0, 0};
+  int perr = 0;
   // fresh simplex slots come from a per-warp chunk kept across launches
   const int gw = blockIdx.x * 4 + wib;
-  int2 chunk = gw < T.cap_wchunk ? T.wchunk[gw] : make_int2(0, 0);
+  int2 chunk = (MODE != 2 && gw < T.cap_wchunk) ? T.wchunk[gw] : make_int2(0, 0);
   const int nw = gridDim.x * 4;
-  const int nin = T.ctr->nwl[sin];
-  for (int it = blockIdx.x * 4 + wib; it < nin; it += nw) {
-    const int c = T.wl[sin & 1][it];
+  const int lo = MODE == 2 ? T.ctr->win_lo : 0;
+  const int nin = MODE == 2 ? T.ctr->nwin : T.ctr->nwl[sin];
+  for (int it = lo + blockIdx.x * 4 + wib; it < nin; it += nw) {
+    const int c = MODE == 2 ? T.win[it] : T.wl[sin & 1][it];
     const int4 info = T.cinfo[c];
-    if (info.w != ST_OK) continue;
+    if (info.w != (MODE == 2 ? ST_WIN : ST_OK)) continue;
     const int4 cd = T.cand[c];
     const unsigned long long key = pe | (unsigned)cd.z;
     int *P, *F, ncav, nfac;
     bool big;
     cand_lists(T, info, P, F, ncav, nfac, big);
-    bool ok = true;
-    for (int i = lane; i < ncav; i += 32) {
-      const int s = P[i];
-      if (bad_simp(T, s)) {
-        ok = false;
+    int base;
+    if (MODE != 2) {
+      bool ok = true;
+      for (int i = lane; i < ncav; i += 32) {
+        const int s = P[i];
+        if (bad_simp(T, s)) {
+          ok = false;
+          continue;
+        }
+        ok = ok && T.claim_c[s] == key && (MODE == 1 || T.claim_n[s] > key);
+      }
+      for (int j = lane; j < nfac && ok; j += 32) {
+        const int o = F[6 * j + 4];
+        if (o < 0) continue;
+        if (bad_simp(T, o >> 2)) {
+          ok = false;
+          continue;
+        }
+        const unsigned long long ko = T.claim_c[o >> 2];
+        if (MODE == 0) {
+          ok = ko > key;
+        } else if (ko < key) {
+          // the lower candidate X whose cavity holds the outer simplex
+          const int xv = (int)vertex_of_priority((uint32_t)ko, seed);
+          if (bad_vert(T, xv)) {
+            ok = false;
+            continue;
+          }
+          const int* r = F + 6 * j;
+          vdp::FPt fv[NV];
+          for (int i = 0; i < NV; ++i) fv[i] = load_fpt(T, r[i]);
+          const vdp::FPt fx = load_fpt(T, xv);
+          auto load64 = [&](vdp::VPt* v64, vdp::VPt& p64) {
+            for (int i = 0; i < NV; ++i) v64[i] = load_pt(T, r[i]);
+            p64 = load_pt(T, xv);
+          };
+          ok = !vdp::in_conflict_hl<D>(fv, r, fx, xv, tl, perr, load64);
+        }
+      }
+      if (!__all_sync(FULL, ok)) {
+        if (lane == 0) {
+          if (last) {
+            T.cinfo[c].w = ST_LOST;
+          } else {
+            const int k = atomicAdd(&T.ctr->nwl[sout], 1);
+            T.wl[sout & 1][k] = c;
+          }
+        }
         continue;
       }
-      ok = ok && T.claim_c[s] == key && T.claim_n[s] > key;
-    }
-    for (int j = lane; j < nfac; j += 32) {
-      const int o = F[6 * j + 4];
-      if (o < 0) continue;
-      ok = ok && !bad_simp(T, o >> 2) && T.claim_c[o >> 2] > key;
-    }
-    if (!__all_sync(FULL, ok)) {
-      if (lane == 0) {
-        if (last) {
-          T.cinfo[c].w = ST_LOST;
-        } else {
-          const int k = atomicAdd(&T.ctr->nwl[sout], 1);
-          T.wl[sout & 1][k] = c;
+      const int fresh = max(0, nfac - ncav);
+      if (fresh > chunk.y) {
+        const int take = max(fresh, kSlotChunk);
+        int b0 = 0;
+        if (lane == 0) b0 = atomicAdd(&T.ctr->nsimp, take);
+        b0 = __shfl_sync(FULL, b0, 0);
+        chunk = make_int2(b0, take);
+        if (b0 + take > T.cap_simp) {
+          if (lane == 0) {
+            atomicAdd(&T.ctr->wasted, take);
+            atomicExch(&T.ctr->simp_overflow, 1);
+          }
+          chunk = make_int2(0, 0);
         }
       }
-      continue;
-    }
-    const int fresh = max(0, nfac - ncav);
-    if (fresh > chunk.y) {
-      const int take = max(fresh, kSlotChunk);
-      int b0 = 0;
-      if (lane == 0) b0 = atomicAdd(&T.ctr->nsimp, take);
-      b0 = __shfl_sync(FULL, b0, 0);
-      chunk = make_int2(b0, take);
-      if (b0 + take > T.cap_simp) {
+      if (fresh > chunk.y) {
+        if (lane == 0) T.cinfo[c].w = ST_LOST;
+        continue;
+      }
+      base = chunk.x;
+      chunk.x += fresh;
+      chunk.y -= fresh;
+      for (int i = lane; i < ncav; i += 32) T.killed[P[i]] = make_int2(round, cd.x);
+      ++nwon;
+      if (MODE == 1) {
         if (lane == 0) {
-          atomicAdd(&T.ctr->wasted, take);
-          atomicExch(&T.ctr->simp_overflow, 1);
+          T.cand[c].y = base;  // the home simplex is not needed any more
+          T.cinfo[c].w = ST_WIN;
+          T.win[atomicAdd(&T.ctr->nwin, 1)] = c;
         }
-        chunk = make_int2(0, 0);
+        __syncwarp();
+        continue;
       }
+    } else {
+      base = cd.y;
     }
-    if (fresh > chunk.y) {
-      if (lane == 0) T.cinfo[c].w = ST_LOST;
-      continue;
-    }
-    const int base = chunk.x;
-    chunk.x += fresh;
-    chunk.y -= fresh;
-    for (int i = lane; i < ncav; i += 32) T.killed[P[i]] = make_int2(round, cd.x);
     int id0;
+    const int* IDS;
     if (!big && nfac <= MAXF && ncav <= MAXC) {
       // slot assignment: first facet of cavity simplex k takes k's slot;
       // the other facets take the remaining cavity slots, then fresh ones
@@ -1079,6 +1137,7 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last) {
       }
       __syncwarp();
       id0 = W.id[0];
+      IDS = W.id;
       // leftover cavity slots become holes pointing into the star
       for (int t = nsec + lane; t < nfree; t += 32)
         store_simplex(T, W.freeslot[t], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
@@ -1091,30 +1150,77 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last) {
       for (int j = lane; j < nfac; j += 32) ID[j] = j < ncav ? P[j] : base + (j - ncav);
       __syncwarp();
       id0 = ID[0];
+      IDS = ID;
       for (int i = nfac + lane; i < ncav; i += 32)
         store_simplex(T, P[i], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
       write_star_big<D>(T, F, ID, nfac, round, P + kOffR, lane);
+    }
+    if (MODE == 2) {
+      // facets shared with another winner's cavity: publish this side's new
+      // simplex and remember where the other side's goes (k_fix_links)
+      __syncwarp();
+      for (int j = lane; j < nfac; j += 32) {
+        const int o = F[6 * j + 4];
+        if (o < 0 || bad_simp(T, o >> 2) || T.killed[o >> 2].x != round) continue;
+        const int kf = F[6 * j + 5], qf = kf & 3, k = kf >> 2;
+        const int inner = (P[k] << 2) | (kf & 3);  // the removed simplex and its face on this facet
+        (void)qf;
+        T.repl[inner] = (IDS[j] << 2) | (kf & 3);
+        F[6 * j] = IDS[j];
+        F[6 * j + 1] = kf & 3;
+        F[6 * j + 2] = -2;
+      }
     }
     if (lane == 0) {
       write_hints<D>(T, cd.x, load_pt(T, cd.x), id0);
       T.cinfo[c].w = ST_DONE;
       T.act[par][cd.w].x = -1;
     }
-    ++nwon;
     ncreated += nfac;
     nkilled += ncav;
     nholes += max(0, ncav - nfac);
     __syncwarp();
   }
+  if (perr) set_error(T.ctr, E_PRECISION);
+  if (MODE == 1) flush_tally(T.ctr, tl, 0, 0);
   if (lane == 0) {
-    if (gw < T.cap_wchunk) T.wchunk[gw] = chunk;
+    if (MODE != 2 && gw < T.cap_wchunk) T.wchunk[gw] = chunk;
     if (nwon) {
       atomicAdd(&T.ctr->won[min(pass, kPassesMax - 1)], nwon);
       atomicAdd(&T.ctr->winners, (int)nwon);
       atomicAdd(&T.ctr->ninserted, (int)nwon);
+    }
+    if (ncreated) {
       atomicAdd(&T.ctr->created, ncreated);
       atomicAdd(&T.ctr->killed, nkilled);
       if (nholes) atomicAdd(&T.ctr->holes, nholes);
+    }
+  }
+}
+
+// Adjacent mode, end of a round: a new simplex whose outer neighbour another
+// winner removed takes, as that neighbour, the other winner's new simplex on
+// the same facet.
+__global__ void k_fix_links(DevTree T) {
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int n = T.ctr->nwin;
+  const long long nrepl = 4LL * T.cap_simp;
+  for (int it = blockIdx.x * (blockDim.x >> 5) + wib; it < n; it += nw) {
+    const int c = T.win[it];
+    const int4 info = T.cinfo[c];
+    if (info.w != ST_DONE) continue;
+    int *P, *F, ncav, nfac;
+    bool big;
+    cand_lists(T, info, P, F, ncav, nfac, big);
+    for (int j = lane; j < nfac; j += 32) {
+      if (F[6 * j + 2] != -2) continue;
+      const int id = F[6 * j], g = F[6 * j + 1], o = F[6 * j + 4];
+      if (bad_simp(T, id) || o < 0 || o >= nrepl) {
+        set_error(T.ctr, E_INTERNAL);
+        continue;
+      }
+      reinterpret_cast<int*>(T.simp + id)[4 + g] = T.repl[o];
     }
   }
 }
@@ -1124,8 +1230,9 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last) {
 // neighbour a winner removed, drops out for this round; the others claim
 // again with this pass's key (smaller than every earlier key of the round).
 template <int D>
-__global__ void __launch_bounds__(128) k_reclaim(DevTree T, int pass) {
+__global__ void __launch_bounds__(128) k_reclaim(DevTree T, int pass, int adjacent) {
   const int round = T.ctr->round;
+  if (blockIdx.x == 0 && threadIdx.x == 0) T.ctr->win_lo = T.ctr->nwin;  // winners of this pass start here
   const int sin = 2 * pass - 1, sout = 2 * pass;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nc = min(T.ctr->ncand, T.cap_cand);
@@ -1153,7 +1260,7 @@ __global__ void __launch_bounds__(128) k_reclaim(DevTree T, int pass) {
       if (lane == 0) T.cinfo[c].w = ST_LOST;
       continue;
     }
-    claim_region(T, P, ncav, F, nfac, pe | (unsigned)cd.z, lane);
+    claim_region(T, P, ncav, F, nfac, pe | (unsigned)cd.z, lane, adjacent);
     if (lane == 0) {
       const int k = atomicAdd(&T.ctr->nwl[sout], 1);
       T.wl[sout & 1][k] = c;
@@ -1250,7 +1357,7 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
     }
   };
   if (pf && pf->n == 0) cudaEventRecord(pf->ev[0], L.stream);
-  note_launches(6 + 2 * tu.passes - 1);
+  note_launches(tu.adjacent ? 7 + 3 * tu.passes - 1 : 6 + 2 * tu.passes - 1);
   k_plan<<<1, 32, 0, L.stream>>>(T, fd.ratio);
   k_activate<D><<<L.blocks, 256, 0, L.stream>>>(T, fd.seed);
   mark(KT_ACTIVATE);
@@ -1258,17 +1365,24 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
   mark(KT_PICK);
   k_thin<D><<<L.blocks, 256, 0, L.stream>>>(T, tu.thin);
   mark(KT_THIN);
-  k_cavity<D><<<L.warps / 4, 128, 0, L.stream>>>(T);
+  k_cavity<D><<<L.warps / 4, 128, 0, L.stream>>>(T, tu.adjacent);
   mark(KT_CAVITY);
+  const int commit_grid = std::min(L.warps / 4, g_check_wave[D - 2]);
   for (int p = 0; p < tu.passes; ++p) {
+    const int last = p == tu.passes - 1;
     if (p > 0) {
-      k_reclaim<D><<<L.warps / 4, 128, 0, L.stream>>>(T, p);
+      k_reclaim<D><<<L.warps / 4, 128, 0, L.stream>>>(T, p, tu.adjacent);
       mark(KT_RECLAIM);
     }
-    k_check<D><<<std::min(L.warps / 4, g_check_wave[D - 2]), 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(
-        T, p, p == tu.passes - 1);
+    if (tu.adjacent) {
+      k_check<D, 1><<<L.warps / 4, 128, 0, L.stream>>>(T, p, last, fd.seed);
+      k_check<D, 2><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
+    } else {
+      k_check<D, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
+    }
     mark(KT_CHECK);
   }
+  if (tu.adjacent) k_fix_links<<<L.warps / 4, 128, 0, L.stream>>>(T);
   k_relocate<D><<<L.blocks, 256, 0, L.stream>>>(T);
   mark(KT_RELOCATE);
 }
@@ -1298,17 +1412,22 @@ void launch_levels(const DevTree& T, const Launch& L, int64_t n, int base_vid, u
 
 namespace {
 int prepare_once() {
-  const cudaError_t e3 = cudaFuncSetAttribute(k_check<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              4 * (int)sizeof(WarpCommit<3>));
-  const cudaError_t e2 = cudaFuncSetAttribute(k_check<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              4 * (int)sizeof(WarpCommit<2>));
-  if (e3 != cudaSuccess || e2 != cudaSuccess) return E_CUDA;
+  cudaError_t e = cudaSuccess;
+  auto attr = [&](const void* f, int bytes) {
+    const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (r != cudaSuccess) e = r;
+  };
+  attr((const void*)k_check<3, 0>, 4 * (int)sizeof(WarpCommit<3>));
+  attr((const void*)k_check<3, 2>, 4 * (int)sizeof(WarpCommit<3>));
+  attr((const void*)k_check<2, 0>, 4 * (int)sizeof(WarpCommit<2>));
+  attr((const void*)k_check<2, 2>, 4 * (int)sizeof(WarpCommit<2>));
+  if (e != cudaSuccess) return E_CUDA;
   // k_check is a grid-stride loop: one resident wave avoids a ragged second
   int dev = 0, sms = 0, b3 = 0, b2 = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_check<3>, 128, 4 * sizeof(WarpCommit<3>)) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_check<2>, 128, 4 * sizeof(WarpCommit<2>)) != cudaSuccess)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_check<3, 0>, 128, 4 * sizeof(WarpCommit<3>)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_check<2, 0>, 128, 4 * sizeof(WarpCommit<2>)) != cudaSuccess)
     return E_CUDA;
   g_check_wave[1] = std::max(1, sms * b3);
   g_check_wave[0] = std::max(1, sms * b2);

@@ -160,7 +160,7 @@ struct vd_tree {
   std::vector<vd::Prof> profs;   // one event log per round of a chunk
   double kms[vd::KT_COUNT] = {};
   int64_t kcnt[vd::KT_COUNT] = {};
-  vd::Tuning tuning = {2, 2};
+  vd::Tuning tuning = {2, 2, 1};
   // per-round trace (diagnostics; syncs after every round)
   bool trace = false;
   std::vector<int64_t> trace_rows;
@@ -168,7 +168,7 @@ struct vd_tree {
   // bakes in (the device tree by value, grid, tuning and feed)
   struct ChunkGraph {
     vd::DevTree T;
-    int chunk, blocks, warps, passes, thin;
+    int chunk, blocks, warps, passes, thin, adjacent;
     uint64_t seed;
     float ratio;
     long long launches;
@@ -297,6 +297,8 @@ int ensure_simplices(vd_tree* t, int64_t want) {
   rc |= grow(&t->T.claim_n, &c[4], want, used, 0xff, t->stream);
   rc |= grow(&t->T.killed, &c[5], want, used, 0xff, t->stream);
   rc |= grow(&t->T.touched, &c[6], want, used, 0xff, t->stream);
+  int64_t cr = 4 * cap;  // read only where written in the same round
+  rc |= grow(&t->T.repl, &cr, 4 * want, 0, -1, t->stream);
   if (rc) return vd::E_NOMEM;
   t->T.cap_simp = (int)want;
   return vd::E_OK;
@@ -323,9 +325,10 @@ int ensure_points(vd_tree* t, int64_t n_new) {
     dfree(t->T.wl[0]);
     dfree(t->T.wl[1]);
     dfree(t->T.order);
+    dfree(t->T.win);
     if (dalloc(&t->T.act[0], c) || dalloc(&t->T.act[1], c) || dalloc(&t->T.cand, c) ||
         dalloc(&t->T.cinfo, c) || dalloc(&t->T.wl[0], c) || dalloc(&t->T.wl[1], c) ||
-        dalloc(&t->T.order, c))
+        dalloc(&t->T.order, c) || dalloc(&t->T.win, c))
       return vd::E_NOMEM;
     t->cap_act = c;
     t->T.cap_cand = (int)c;
@@ -377,6 +380,8 @@ void release(vd_tree* t) {
   dfree(t->T.act[0]);
   dfree(t->T.act[1]);
   dfree(t->T.order);
+  dfree(t->T.win);
+  dfree(t->T.repl);
   dfree(t->T.cand);
   dfree(t->T.cinfo);
   dfree(t->T.wl[0]);
@@ -446,7 +451,7 @@ int ensure_sets(vd_tree* t, int64_t nsets) {
 int alloc_tree(vd_tree* t, int dim, void* stream) {
   t->dim = dim;
   t->ns = dim + 1;
-  t->tuning = dim == 3 ? vd::Tuning{2, 2} : vd::Tuning{3, 1};
+  t->tuning = dim == 3 ? vd::Tuning{2, 2, 1} : vd::Tuning{2, 1, 1};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return vd::E_CUDA;
   t->device = dev;
@@ -686,7 +691,7 @@ bool launch_chunk_graph(vd_tree* t, const vd::Launch& L, int chunk, const vd::Fe
   vd_tree::ChunkGraph* hit = nullptr;
   for (auto& g : t->graphs)
     if (g.chunk == chunk && g.blocks == L.blocks && g.warps == L.warps && g.passes == t->tuning.passes &&
-        g.thin == t->tuning.thin && g.seed == fd.seed && g.ratio == fd.ratio &&
+        g.thin == t->tuning.thin && g.adjacent == t->tuning.adjacent && g.seed == fd.seed && g.ratio == fd.ratio &&
         memcmp(&g.T, &t->T, sizeof(vd::DevTree)) == 0) {
       hit = &g;
       break;
@@ -717,6 +722,7 @@ bool launch_chunk_graph(vd_tree* t, const vd::Launch& L, int chunk, const vd::Fe
     g.warps = L.warps;
     g.passes = t->tuning.passes;
     g.thin = t->tuning.thin;
+    g.adjacent = t->tuning.adjacent;
     g.seed = fd.seed;
     g.ratio = fd.ratio;
     g.launches = launches;
@@ -1406,6 +1412,12 @@ int vd_set_tuning(vd_tree* t, int passes, int thin) {
   return VD_OK;
 }
 
+int vd_set_adjacent(vd_tree* t, int on) {
+  if (ready(t)) return VD_ERR_ARG;
+  t->tuning.adjacent = on ? 1 : 0;
+  return VD_OK;
+}
+
 int vd_set_graphs(vd_tree* t, int on) {
   if (ready(t)) return VD_ERR_ARG;
   t->use_graphs = on != 0;
@@ -1532,7 +1544,7 @@ int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, i
                     sizeof(double) * (offsets[pick[i] + 1] - offsets[pick[i]]) * dim, cudaMemcpyDeviceToDevice,
                     t->stream);
   struct Cfg {
-    int wps, bps, passes, thin;
+    int wps, bps, passes, thin, adjacent;
     double ratio;
   };
   std::vector<int64_t> eoff(ns + 1);
@@ -1545,6 +1557,7 @@ int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, i
     t->blocks_per_sm = c.bps;
     t->tuning.passes = c.passes;
     t->tuning.thin = c.thin;
+    t->tuning.adjacent = c.adjacent;
     t->ratio = c.ratio;
   };
   auto time_cfg = [&](const Cfg& c) -> double {
@@ -1568,7 +1581,7 @@ int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, i
     }
     return best;
   };
-  Cfg best{t->warps_per_sm, t->blocks_per_sm, t->tuning.passes, t->tuning.thin, t->ratio};
+  Cfg best{t->warps_per_sm, t->blocks_per_sm, t->tuning.passes, t->tuning.thin, t->tuning.adjacent, t->ratio};
   double best_ms = time_cfg(best);
   // coordinate descent, one sweep per coordinate
   const int wps_c[] = {8, 12, 16, 20, 24, 28, 32};
@@ -1576,6 +1589,7 @@ int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, i
   const int pass_c[] = {1, 2, 3};
   const int thin_c[] = {1, 2};
   const double ratio_c[] = {0.06, 0.12, 0.25, 0.5};
+  const int adj_c[] = {0, 1};
   auto sweep = [&](auto field, const auto& values) {
     for (const auto& v : values) {
       if (rc) return;
@@ -1588,6 +1602,7 @@ int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, i
       }
     }
   };
+  sweep([](Cfg& c, int v) { c.adjacent = v; }, adj_c);
   sweep([](Cfg& c, double v) { c.ratio = v; }, ratio_c);
   sweep([](Cfg& c, int v) { c.passes = v; }, pass_c);
   sweep([](Cfg& c, int v) { c.thin = v; }, thin_c);
@@ -1608,6 +1623,7 @@ int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, i
     out[5] = (int64_t)(best_ms * 1000.0);
     out[6] = npts;
     out[7] = ns;
+    out[8] = best.adjacent;
   }
   return rc;
 }

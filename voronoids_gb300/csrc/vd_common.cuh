@@ -36,7 +36,7 @@ struct alignas(32) Simplex {
 };
 
 // Per-round statuses of a candidate.
-enum : int { ST_OK = 0, ST_DUP = 1, ST_OVERFLOW = 2, ST_POOL = 3, ST_LOST = 4, ST_DONE = 5 };
+enum : int { ST_OK = 0, ST_DUP = 1, ST_OVERFLOW = 2, ST_POOL = 3, ST_LOST = 4, ST_DONE = 5, ST_WIN = 6 };
 
 // Resolution passes per round (independent-set refinement), see vd_build.cu.
 constexpr int kPassesMax = 6;
@@ -92,6 +92,7 @@ struct Counters {
   int nlev;                         // levels of the current call
   int feed_lo, feed_hi;             // range of `order` activated this round
   int round;                        // round being run (advanced by k_plan)
+  int nwin, win_lo;                 // winners of the round (adjacent mode), first of the pass
 };
 
 // Points of one insertion call are split into priority levels of
@@ -132,6 +133,8 @@ struct DevTree {
   int4* cand;     // (vid, loc, priority, active slot)
   int4* cinfo;    // (ncav, nfac, pool offset, status)
   int* wl[2];     // work lists (candidate indices), stage s in wl[s & 1]
+  int* win;       // winners of the round (adjacent mode)
+  int* repl;      // per (slot << 2 | face): new simplex code on that face (adjacent mode)
   int* pool;
   int2* dups;     // (dropped vid, vid it equals)
   Counters* ctr;
@@ -174,6 +177,20 @@ __host__ __device__ inline uint32_t priority(uint32_t vid, uint64_t seed) {
   x = mix32(x);
   x ^= (uint32_t)(seed >> 32);
   return mix32(x);
+}
+// Inverse of mix32: each xor-shift and odd multiplication is undone in
+// reverse order (multiplicative inverses modulo 2^32 of the two constants).
+__host__ __device__ inline uint32_t unmix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x43021123U;  // inverse of 0x846ca68b
+  x ^= (x >> 15) ^ (x >> 30);
+  x *= 0x1d69e2a5U;  // inverse of 0x7feb352d
+  x ^= x >> 16;
+  return x;
+}
+// The vertex id with priority `pr` under `seed`.
+__host__ __device__ inline uint32_t vertex_of_priority(uint32_t pr, uint64_t seed) {
+  return unmix32(unmix32(pr) ^ (uint32_t)(seed >> 32)) ^ (uint32_t)seed;
 }
 
 #if defined(__CUDACC__)
@@ -221,6 +238,7 @@ struct Feed {
 struct Tuning {
   int passes;
   int thin;
+  int adjacent;  // 1: cavities of one pass may touch (see k_check in vd_build.cu)
 };
 // Kernel types for profiling.
 enum { KT_PICK, KT_THIN, KT_CAVITY, KT_CHECK, KT_RECLAIM, KT_RELOCATE, KT_ACTIVATE, KT_EDGES, KT_COUNT };
@@ -228,7 +246,7 @@ extern const char* const kKernelTypeNames[KT_COUNT];
 // Event log of one round: ev[0] before the first kernel, ev[i + 1] after
 // kernel i, whose type is type[i].
 struct Prof {
-  static constexpr int kMax = 5 + 2 * kPassesMax;
+  static constexpr int kMax = 5 + 3 * kPassesMax;
   cudaEvent_t ev[kMax + 1];
   int type[kMax];
   int n;

@@ -135,13 +135,13 @@ class DelaunayTree:
         """Tune launch shape and round settings on a sample of a device batch;
         returns the chosen setting."""
         off = np.ascontiguousarray(offsets, dtype=np.int64)
-        out = np.zeros(8, dtype=np.int64)
+        out = np.zeros(9, dtype=np.int64)
         i64p = ctypes.POINTER(ctypes.c_int64)
         _check(_native.load().vd_autotune_batch(self._h, ctypes.c_void_p(ptr), off.ctypes.data_as(i64p),
                                                  off.shape[0] - 1, int(sample_points), out.ctypes.data_as(i64p)),
                "autotune_batch")
         keys = ("warps_per_sm", "blocks_per_sm", "passes", "thin", "ratio_x1000", "sample_us", "sample_points",
-                "sample_sets")
+                "sample_sets", "adjacent")
         return dict(zip(keys, out.tolist()))
 
     def locate(self, points):
@@ -281,6 +281,10 @@ class DelaunayTree:
 
     def set_tuning(self, passes=3, thin=1):
         _check(_native.load().vd_set_tuning(self._h, int(passes), int(thin)), "set_tuning")
+
+    def set_adjacent(self, on=True):
+        """Round mode: 1 lets touching cavities win together (see vd_set_adjacent)."""
+        _check(_native.load().vd_set_adjacent(self._h, int(on)), "set_adjacent")
 
     def set_graphs(self, on=True):
         _check(_native.load().vd_set_graphs(self._h, int(on)), "set_graphs")
