@@ -130,6 +130,13 @@ int vd_max_simplex_id(vd_tree* t, int64_t* id);
 int vd_num_simplices(vd_tree* t, int64_t* n);
 int vd_simplices(vd_tree* t, int32_t* verts, int32_t* nbrs, int64_t cap, int64_t* n);
 
+/* Circumcentre and radius of every live simplex, in vd_simplices order
+ * (PySimplex.center / .radius of the reference's dictionary view,
+ * src/lib.rs:32-59; computed in FP64 on the GPU for the final simplices,
+ * which the reference computes in floating point too, src/geometry.rs:2-56).
+ * centers: 3 doubles per simplex (z = 0 in 2D).  *n receives the count. */
+int vd_circumspheres(vd_tree* t, double* centers, double* radii, int64_t cap, int64_t* n);
+
 /* Sorted Delaunay edge list among inserted points. */
 int vd_num_edges(vd_tree* t, int64_t* n);
 int vd_edges(vd_tree* t, int64_t* uv, int64_t cap, int64_t* n);

@@ -1700,6 +1700,44 @@ int vd_locate_points(vd_tree* t, const double* pts, int64_t nq, int64_t* offsets
   return outside ? VD_ERR_OUTSIDE : VD_OK;
 }
 
+int vd_circumspheres(vd_tree* t, double* centers, double* radii, int64_t cap, int64_t* n) {
+  if (ready(t) || !t->has_geometry || !n) return VD_ERR_ARG;
+  int rc = sync_counters(t);
+  if (rc) return rc;
+  const int nsimp = t->hctr->nsimp;
+  const vd::Launch L = launch_of(t);
+  int *flags = nullptr, *rank = nullptr, *tmp = nullptr;
+  if (dalloc(&flags, nsimp + 1) || dalloc(&rank, nsimp + 1) || dalloc(&tmp, vd::scan_scratch_ints(nsimp + 1))) {
+    dfree(flags);
+    dfree(rank);
+    return VD_ERR_NOMEM;
+  }
+  vd::launch_live_rank(t->T, L, nsimp, flags, rank, tmp);
+  int live = 0;
+  cudaMemcpyAsync(&live, rank + nsimp, sizeof(int), cudaMemcpyDeviceToHost, t->stream);
+  rc = cuda_status(cudaStreamSynchronize(t->stream));
+  *n = live;
+  if (!rc && (centers || radii)) {
+    double *dc = nullptr, *dr = nullptr;
+    if (cap < live || !centers || !radii) {
+      rc = VD_ERR_ARG;
+    } else if (dalloc(&dc, 3 * (size_t)live + 3) || dalloc(&dr, (size_t)live + 1)) {
+      rc = VD_ERR_NOMEM;
+    } else {
+      vd::launch_circum(t->T, L, t->dim, nsimp, rank, dc, dr);
+      cudaMemcpyAsync(centers, dc, sizeof(double) * 3 * live, cudaMemcpyDeviceToHost, t->stream);
+      cudaMemcpyAsync(radii, dr, sizeof(double) * live, cudaMemcpyDeviceToHost, t->stream);
+      rc = cuda_status(cudaStreamSynchronize(t->stream));
+    }
+    dfree(dc);
+    dfree(dr);
+  }
+  dfree(flags);
+  dfree(rank);
+  dfree(tmp);
+  return rc;
+}
+
 int vd_locate(vd_tree* t, const double* p, int64_t* out, int64_t cap, int64_t* n) {
   if (!n) return VD_ERR_ARG;
   int64_t off[2] = {0, 0};

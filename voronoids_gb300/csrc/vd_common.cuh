@@ -282,6 +282,10 @@ void scan_ints(const int* in, int* out, int64_t n, int* tmp, cudaStream_t st);
 void launch_locate(const DevTree& T, const Launch& L, int dim, const double* d_q, int nq, int cap_per,
                    const int* rank, int* out, int* counts);
 void launch_live_rank(const DevTree& T, const Launch& L, int nsimp, int* flags, int* rank, int* tmp);
+// Circumcentre (3 doubles, z = 0 in 2D) and radius of each live simplex,
+// written at its rank.
+void launch_circum(const DevTree& T, const Launch& L, int dim, int nsimp, const int* rank, double* centers,
+                   double* radii);
 void launch_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_in,
                   const EdgeScratch& S, uint2* d_out);
 

@@ -137,7 +137,57 @@ __global__ void k_live_flags(DevTree T, int nsimp, int* flags) {
     flags[s] = T.simp[s].v[0] >= 0 ? 1 : 0;
 }
 
+// Circumsphere of every live simplex, in the order of the simplex export
+// (rank), for the dictionary view of the reference (PySimplex.center and
+// .radius, src/lib.rs:32-59).  FP64 closed form relative to vertex 0:
+// 3D c = p0 + (|a|^2 (b x c) + |b|^2 (c x a) + |c|^2 (a x b)) / (2 a.(b x c)),
+// 2D the same in the plane.  These are floating-point values (the reference's
+// own are too, src/geometry.rs:2-56); the triangulation never uses them.
+template <int D>
+__global__ void k_circum(DevTree T, int nsimp, const int* rank, double* centers, double* radii) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsimp; s += gridDim.x * blockDim.x) {
+    const int4 v = reinterpret_cast<const int4*>(T.simp + s)[0];
+    if (v.x < 0) continue;
+    const int o = rank[s];
+    const vdp::VPt p0 = T.pts[v.x], p1 = T.pts[v.y], p2 = T.pts[v.z];
+    double cx, cy, cz = 0.0;
+    if (D == 3) {
+      const vdp::VPt p3 = T.pts[v.w];
+      const double ax = p1.x - p0.x, ay = p1.y - p0.y, az = p1.z - p0.z;
+      const double bx = p2.x - p0.x, by = p2.y - p0.y, bz = p2.z - p0.z;
+      const double qx = p3.x - p0.x, qy = p3.y - p0.y, qz = p3.z - p0.z;
+      const double a2 = ax * ax + ay * ay + az * az, b2 = bx * bx + by * by + bz * bz, q2 = qx * qx + qy * qy + qz * qz;
+      const double bcx = by * qz - bz * qy, bcy = bz * qx - bx * qz, bcz = bx * qy - by * qx;
+      const double cax = qy * az - qz * ay, cay = qz * ax - qx * az, caz = qx * ay - qy * ax;
+      const double abx = ay * bz - az * by, aby = az * bx - ax * bz, abz = ax * by - ay * bx;
+      const double den = 2.0 * (ax * bcx + ay * bcy + az * bcz);
+      cx = (a2 * bcx + b2 * cax + q2 * abx) / den;
+      cy = (a2 * bcy + b2 * cay + q2 * aby) / den;
+      cz = (a2 * bcz + b2 * caz + q2 * abz) / den;
+    } else {
+      const double ax = p1.x - p0.x, ay = p1.y - p0.y, bx = p2.x - p0.x, by = p2.y - p0.y;
+      const double a2 = ax * ax + ay * ay, b2 = bx * bx + by * by;
+      const double den = 2.0 * (ax * by - ay * bx);
+      cx = (by * a2 - ay * b2) / den;
+      cy = (ax * b2 - bx * a2) / den;
+    }
+    centers[3LL * o] = p0.x + cx;
+    centers[3LL * o + 1] = p0.y + cy;
+    centers[3LL * o + 2] = D == 3 ? p0.z + cz : 0.0;
+    radii[o] = sqrt(cx * cx + cy * cy + cz * cz);
+  }
+}
+
 }  // namespace
+
+void launch_circum(const DevTree& T, const Launch& L, int dim, int nsimp, const int* rank, double* centers,
+                   double* radii) {
+  note_launches(1);
+  if (dim == 3)
+    k_circum<3><<<L.blocks, 256, 0, L.stream>>>(T, nsimp, rank, centers, radii);
+  else
+    k_circum<2><<<L.blocks, 256, 0, L.stream>>>(T, nsimp, rank, centers, radii);
+}
 
 void launch_locate(const DevTree& T, const Launch& L, int dim, const double* d_q, int nq, int cap_per,
                    const int* rank, int* out, int* counts) {
