@@ -39,10 +39,10 @@ N_POINTS = 1_000_000
 SEED = 0x5EED
 CPU_SAMPLE = 200_000
 
-# Algorithmic bytes per unit: k_cavity moves one 32-byte
-# simplex record and four 32-byte split-coordinate records per conflict test;
-# k_check reads a candidate's claims and lists (~1264 B) and a winner writes
-# its star (~1240 B).
+# Algorithmic bytes per unit: k_cavity moves one 32-byte simplex record and
+# four 32-byte split-coordinate records per conflict test; the decide half of
+# the check reads a candidate's claims and lists (~1264 B) and the commit half
+# writes a winner's star (~1240 B).
 BYTES_PER_TEST_3D = 160
 BYTES_PER_CHECK = 1264
 BYTES_PER_WIN = 1240
@@ -582,8 +582,10 @@ def main():
     tests = stats["cavity_tests"]
     if dname == "k_cavity":
         algo_bytes = BYTES_PER_TEST_3D * tests * args.steps
-    elif dname == "k_check":
-        algo_bytes = (BYTES_PER_CHECK * stats["searched"] + BYTES_PER_WIN * stats["inserted"]) * args.steps
+    elif dname == "k_check":  # adjacent mode: the commit half (stars of the winners)
+        algo_bytes = BYTES_PER_WIN * stats["inserted"] * args.steps
+    elif dname == "k_decide":  # adjacent mode: claims and lists of every searched candidate
+        algo_bytes = BYTES_PER_CHECK * stats["searched"] * args.steps
     else:
         algo_bytes = None
     peak, peak_kind = measured_peaks()

@@ -162,7 +162,7 @@ const char* vd_status_str(int status);
  * println!, src/delaunay_tree.rs:337-368).  Profiling records CUDA events
  * around every kernel of every round on the tree's stream; vd_profile returns
  * the summed milliseconds and launch counts per kernel (names from
- * vd_profile_name; the last entry is the edge extraction).  Turning it on
+ * vd_profile_name; "edges" is the edge extraction).  Turning it on
  * resets the sums.  The trace synchronises after every round and keeps one
  * row per round: round, active points at start, cumulative nominations,
  * cumulative searches, cumulative insertions, cumulative conflict tests,

@@ -1376,13 +1376,17 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
     }
     if (tu.adjacent) {
       k_check<D, 1><<<L.warps / 4, 128, 0, L.stream>>>(T, p, last, fd.seed);
+      mark(KT_DECIDE);
       k_check<D, 2><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
     } else {
       k_check<D, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
     }
     mark(KT_CHECK);
   }
-  if (tu.adjacent) k_fix_links<<<L.warps / 4, 128, 0, L.stream>>>(T);
+  if (tu.adjacent) {
+    k_fix_links<<<L.warps / 4, 128, 0, L.stream>>>(T);
+    mark(KT_FIX);
+  }
   k_relocate<D><<<L.blocks, 256, 0, L.stream>>>(T);
   mark(KT_RELOCATE);
 }
@@ -1451,6 +1455,7 @@ void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, 
 }
 
 const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_thin",     "k_cavity", "k_check",
-                                                "k_reclaim",  "k_relocate", "k_activate", "edges"};
+                                                "k_reclaim",  "k_relocate", "k_activate", "edges",
+                                                "k_decide",   "k_fix_links"};
 
 }  // namespace vd

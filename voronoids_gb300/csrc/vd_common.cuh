@@ -241,7 +241,19 @@ struct Tuning {
   int adjacent;  // 1: cavities of one pass may touch (see k_check in vd_build.cu)
 };
 // Kernel types for profiling.
-enum { KT_PICK, KT_THIN, KT_CAVITY, KT_CHECK, KT_RECLAIM, KT_RELOCATE, KT_ACTIVATE, KT_EDGES, KT_COUNT };
+enum {
+  KT_PICK,
+  KT_THIN,
+  KT_CAVITY,
+  KT_CHECK,
+  KT_RECLAIM,
+  KT_RELOCATE,
+  KT_ACTIVATE,
+  KT_EDGES,
+  KT_DECIDE,
+  KT_FIX,
+  KT_COUNT
+};
 extern const char* const kKernelTypeNames[KT_COUNT];
 // Event log of one round: ev[0] before the first kernel, ev[i + 1] after
 // kernel i, whose type is type[i].
