@@ -177,8 +177,8 @@ int vd_set_profiling(vd_tree* t, int on);
  * active.  Defaults 64, 1.25 and 0.12. */
 int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth, double ratio);
 /* Round tuning: resolution passes per round (1..6) and the thinning radius
- * (1 = a nominee must hold its simplex and face neighbours, 2 = and no lower
- * nominee two faces away).  Defaults: 3D 2 passes / radius 2, 2D 2 / 1. */
+ * (0 = every nominee is searched, 1 = a nominee must hold its simplex and
+ * face neighbours, 2 = and no lower nominee two faces away).  Defaults: 3D 2 passes / radius 2, 2D 2 / 1. */
 int vd_set_tuning(vd_tree* t, int passes, int thin);
 /* Round mode (no reference counterpart).  0: winners of a pass have
  * disjoint cavities and no cavity touches another's outer shell, the
@@ -187,6 +187,19 @@ int vd_set_tuning(vd_tree* t, int passes, int thin);
  * wins if the shared facets stay locally Delaunay (exact test), and the two
  * stars are stitched after the pass.  Same triangulation either way. */
 int vd_set_adjacent(vd_tree* t, int on);
+/* While the next round would have fewer than `max_active` active points
+ * (default 0 = never), rounds run in one cooperative launch with a
+ * grid barrier between their phases instead of one kernel launch per phase
+ * (the first rounds of a build are latency chains of small kernels).  No
+ * reference counterpart; the triangulation is the same. */
+int vd_set_small_rounds(vd_tree* t, int max_active);
+/* Early phase of a call: until `until_inserted` points of the tree are
+ * inserted, rounds use thinning radius `thin` and a feed ratio of at least
+ * `ratio` (the device is far from busy while the triangulation is small, so
+ * more searches per round cost little and save rounds).  Defaults 10000
+ * points, radius 0, ratio 0.5; until_inserted = 0 turns it off.  No
+ * reference counterpart; the triangulation is the same. */
+int vd_set_early_phase(vd_tree* t, int64_t until_inserted, int thin, double ratio);
 /* Rounds are launched in chunks captured once as CUDA graphs and replayed
  * (default on; profiling and tracing launch kernel by kernel).  No reference
  * counterpart. */

@@ -45,9 +45,17 @@ constexpr unsigned FULL = 0xffffffffu;
 
 template <int D>
 struct Cap;
+#ifndef VD_CAP3_C
+#define VD_CAP3_C 128
+#define VD_CAP3_F 192
+#define VD_CAP3_H 256
+#endif
+#ifndef VD_CAVITY_MIN_BLOCKS
+#define VD_CAVITY_MIN_BLOCKS 5
+#endif
 template <>
 struct Cap<3> {
-  static constexpr int MAXC = 128, MAXF = 192, HS = 256;
+  static constexpr int MAXC = VD_CAP3_C, MAXF = VD_CAP3_F, HS = VD_CAP3_H;
 };
 template <>
 struct Cap<2> {
@@ -304,8 +312,8 @@ __global__ void k_level_order(DevTree T, long long n, int base, unsigned long lo
 // point is active.  Keeping the active set proportional to the triangulation
 // keeps the share of points that win a round high, so few rounds are needed
 // and each point is located and nominated only a few times.
-__global__ void k_plan(DevTree T, float ratio) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void plan_body(DevTree T, float ratio, int bid, int nblk) {
+  if (threadIdx.x != 0 || bid != 0) return;
   Counters* c = T.ctr;
   const int round = c->round + 1;  // the round this launch opens
   c->round = round;
@@ -321,12 +329,13 @@ __global__ void k_plan(DevTree T, float ratio) {
   c->feed_hi = T.lev_off[lev];
   c->lev_next = lev;
 }
+__global__ void k_plan(DevTree T, float ratio) { plan_body(T, ratio, blockIdx.x, gridDim.x); }
 
 // Activates the points planned for this round: each walks from the finest
 // available grid hint to the simplex that contains it (visibility walk,
 // exact orientation), joins the active list and votes for this round.
 template <int D>
-__global__ void k_activate(DevTree T, unsigned long long seed) {
+__device__ __forceinline__ void activate_body(DevTree T, unsigned long long seed, int bid, int nblk) {
   const int round = T.ctr->round;
   constexpr int NV = D + 1;
   const int par = round & 1;
@@ -336,7 +345,7 @@ __global__ void k_activate(DevTree T, unsigned long long seed) {
   int perr = 0;
   unsigned long long walk = 0;
   const int cap = 1 << 16;
-  for (int b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+  for (int b = bid * blockDim.x; b < n; b += nblk * blockDim.x) {
     const int i = b + threadIdx.x;
     const bool act = i < n;
     int cur = 0, vid = 0;
@@ -392,12 +401,14 @@ __global__ void k_activate(DevTree T, unsigned long long seed) {
   if (perr) set_error(T.ctr, E_PRECISION);
   flush_tally(T.ctr, tl, 0, walk);
 }
+template <int D>
+__global__ void k_activate(DevTree T, unsigned long long seed) { activate_body<D>(T, seed, blockIdx.x, gridDim.x); }
 
 // ---------------------------------------------------------------------------
-__global__ void k_pick(DevTree T) {
+__device__ __forceinline__ void pick_body(DevTree T, int thin, int bid, int nblk) {
   const int round = T.ctr->round;
   const int par = round & 1;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (bid == 0 && threadIdx.x == 0) {
     T.ctr->nact[par ^ 1] = 0;
     for (int k = 0; k < kStages; ++k) T.ctr->nwl[k] = 0;
     T.ctr->nwin = 0;
@@ -406,7 +417,7 @@ __global__ void k_pick(DevTree T) {
   const int n = T.ctr->nact[par];
   const unsigned long long ep = epoch(round);
   unsigned long long ncand = 0;
-  for (int b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+  for (int b = bid * blockDim.x; b < n; b += nblk * blockDim.x) {
     int i = b + threadIdx.x;
     bool is = false;
     int4 e = make_int4(-1, 0, 0, 0);
@@ -421,6 +432,7 @@ __global__ void k_pick(DevTree T) {
       // thinning claim: the home simplex and its face neighbours
       const unsigned long long key = ep | (unsigned)e.z;
       int4 v, nn;
+      if (thin == 0) continue;  // every nominee is searched
       load_simplex(T, e.y, v, nn);
       atomicMin(T.thin + e.y, key);
       const int nb[4] = {nn.x, nn.y, nn.z, nn.w};
@@ -431,6 +443,7 @@ __global__ void k_pick(DevTree T) {
   ncand = warp_sum(ncand);
   if ((threadIdx.x & 31) == 0 && ncand) atomicAdd(&T.ctr->candidates, ncand);
 }
+__global__ void k_pick(DevTree T, int thin) { pick_body(T, thin, blockIdx.x, gridDim.x); }
 
 // Storage of one cavity search: shared memory for the common case, a
 // reserved, 16-byte aligned stretch of the round's cavity pool when that
@@ -575,6 +588,7 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
 template <int D>
 __device__ bool thin_lost1(const DevTree& T, int home, int4 n0, unsigned long long key, int thin) {
   constexpr int NV = D + 1;
+  if (thin == 0) return false;
   if (T.thin[home] != key) return true;
   for (int f = 0; f < NV; ++f) {
     const int nb = get4(n0, f);
@@ -599,13 +613,13 @@ __device__ bool thin_lost1(const DevTree& T, int home, int4 n0, unsigned long lo
 // Per nominee (one thread): duplicate test against the vertices of its
 // simplex and the thinning test; survivors go to work list stage 0.
 template <int D>
-__global__ void k_thin(DevTree T, int thin) {
+__device__ __forceinline__ void thin_body(DevTree T, int thin, int bid, int nblk) {
   const int round = T.ctr->round;
   constexpr int NV = D + 1;
   const int nc = min(T.ctr->ncand, T.cap_cand);
   const unsigned long long ep = epoch(round);
   const int par = round & 1;
-  for (int b = blockIdx.x * blockDim.x; b < nc; b += gridDim.x * blockDim.x) {
+  for (int b = bid * blockDim.x; b < nc; b += nblk * blockDim.x) {
     const int c = b + threadIdx.x;
     bool survive = false;
     if (c < nc) {
@@ -633,6 +647,8 @@ __global__ void k_thin(DevTree T, int thin) {
     if (survive) T.wl[0][k] = c;
   }
 }
+template <int D>
+__global__ void k_thin(DevTree T, int thin) { thin_body<D>(T, thin, blockIdx.x, gridDim.x); }
 
 template <int D>
 struct WarpCav {
@@ -658,10 +674,9 @@ __device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int
 }
 
 template <int D>
-__global__ void __launch_bounds__(128) k_cavity(DevTree T, int adjacent) {
+__device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, int nblk, WarpCav<D>* smem) {
   const int round = T.ctr->round;
   constexpr int MAXC = Cap<D>::MAXC, MAXF = Cap<D>::MAXF, HS = Cap<D>::HS;
-  __shared__ WarpCav<D> smem[4];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   WarpCav<D>& W = smem[wib];
   const unsigned long long pe = pass_epoch(round, 0);
@@ -671,12 +686,12 @@ __global__ void __launch_bounds__(128) k_cavity(DevTree T, int adjacent) {
   int mcav = 0, mfac = 0;
   // pool space is taken in per-warp chunks (one atomic per chunk, not per
   // candidate); what a warp leaves unused is dropped with the round's pool
-  const int pchunk = max(256, min(8192, T.cap_pool / (gridDim.x * 16)));
+  const int pchunk = max(256, min(8192, T.cap_pool / (nblk * 16)));
   int pbase = 0, pleft = 0;
   const CavStore fast{W.cav, W.cv, W.cn, W.hkey, W.fr, MAXC, MAXF, HS};
-  const int nw = gridDim.x * 4;
+  const int nw = nblk * 4;
   const int nsurv = T.ctr->nwl[0];
-  for (int it = blockIdx.x * 4 + wib; it < nsurv; it += nw) {
+  for (int it = bid * 4 + wib; it < nsurv; it += nw) {
     const int c = T.wl[0][it];
     const int4 cd = T.cand[c];
     const vdp::VPt q = load_pt(T, cd.x);
@@ -765,6 +780,9 @@ __global__ void __launch_bounds__(128) k_cavity(DevTree T, int adjacent) {
     if (mfac) atomicMax(&T.ctr->max_fac, mfac);
   }
 }
+template <int D>
+__global__ void __launch_bounds__(128, VD_CAVITY_MIN_BLOCKS) k_cavity(DevTree T, int adjacent) { __shared__ WarpCav<D> smem[4];
+  cavity_body<D>(T, adjacent, blockIdx.x, gridDim.x, smem); }
 
 // Pool layout of a searched candidate: cavity ids at P, facet records at
 // P + ncav, or at P + kOffF for a spilled (large) search, flagged by bit 30
@@ -780,7 +798,9 @@ __device__ __forceinline__ void cand_lists(const DevTree& T, const int4& info, i
 
 template <int D>
 struct WarpCommit {
-  static constexpr int HR = D == 3 ? 512 : 256;  // ridge table slots (> 2x ridges)
+  // ridge table slots: a star of f facets has f D / 2 ridges, at most 288
+  // (3D, 192 facets) or 96 (2D, 96 facets): load factor <= 0.75
+  static constexpr int HR = D == 3 ? 512 : 128;
   unsigned long long rk[HR];   // ridge key (r0 << 32 | r1)
   int ra[HR], rb[HR];          // the two half-ridges (facet << 2 | face)
   int id[Cap<D>::MAXF];
@@ -826,7 +846,9 @@ __device__ __forceinline__ void emit_simplex(const DevTree& T, const int* r, int
 template <int D>
 __device__ void write_star(const DevTree& T, WarpCommit<D>& W, const int* __restrict__ FR, int nfac, int qv,
                            int round, int lane) {
-  constexpr int NV = D + 1, HR = WarpCommit<D>::HR;
+  constexpr int NV = D + 1;
+  // table size: a power of two at least twice the ridges, within WarpCommit::HR
+  constexpr int HR = WarpCommit<D>::HR;
   const unsigned long long EMPTY = ~0ull;
   for (int i = lane; i < HR; i += 32) {
     W.rk[i] = EMPTY;
@@ -985,12 +1007,12 @@ __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, i
 // candidates of the pass, so that MODE 2, which writes the stars, knows every
 // simplex removed in the pass and leaves links into them to k_fix_links.
 template <int D, int MODE>
-__global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last, unsigned long long seed) {
+__device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsigned long long seed, int bid, int nblk,
+                                           unsigned char* dsm) {
   constexpr int NV = D + 1;
   const int round = T.ctr->round;
   const int sin = 2 * pass, sout = 2 * pass + 1;
   constexpr int MAXF = Cap<D>::MAXF, MAXC = Cap<D>::MAXC;
-  extern __shared__ __align__(16) unsigned char dsm[];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   WarpCommit<D>& W = reinterpret_cast<WarpCommit<D>*>(dsm)[wib];
   const unsigned long long pe = pass_epoch(round, pass);
@@ -1000,12 +1022,12 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last, un
   vdp::Tally tl = {0, 0, 0, 0};
   int perr = 0;
   // fresh simplex slots come from a per-warp chunk kept across launches
-  const int gw = blockIdx.x * 4 + wib;
+  const int gw = bid * 4 + wib;
   int2 chunk = (MODE != 2 && gw < T.cap_wchunk) ? T.wchunk[gw] : make_int2(0, 0);
-  const int nw = gridDim.x * 4;
+  const int nw = nblk * 4;
   const int lo = MODE == 2 ? T.ctr->win_lo : 0;
   const int nin = MODE == 2 ? T.ctr->nwin : T.ctr->nwl[sin];
-  for (int it = lo + blockIdx.x * 4 + wib; it < nin; it += nw) {
+  for (int it = lo + bid * 4 + wib; it < nin; it += nw) {
     const int c = MODE == 2 ? T.win[it] : T.wl[sin & 1][it];
     const int4 info = T.cinfo[c];
     if (info.w != (MODE == 2 ? ST_WIN : ST_OK)) continue;
@@ -1197,16 +1219,19 @@ __global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last, un
     }
   }
 }
+template <int D, int MODE>
+__global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last, unsigned long long seed) { extern __shared__ __align__(16) unsigned char dsm[];
+  check_body<D, MODE>(T, pass, last, seed, blockIdx.x, gridDim.x, dsm); }
 
 // Adjacent mode, end of a round: a new simplex whose outer neighbour another
 // winner removed takes, as that neighbour, the other winner's new simplex on
 // the same facet.
-__global__ void k_fix_links(DevTree T) {
+__device__ __forceinline__ void fix_body(DevTree T, int bid, int nblk) {
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int nw = nblk * (blockDim.x >> 5);
   const int n = T.ctr->nwin;
   const long long nrepl = 4LL * T.cap_simp;
-  for (int it = blockIdx.x * (blockDim.x >> 5) + wib; it < n; it += nw) {
+  for (int it = bid * (blockDim.x >> 5) + wib; it < n; it += nw) {
     const int c = T.win[it];
     const int4 info = T.cinfo[c];
     if (info.w != ST_DONE) continue;
@@ -1224,22 +1249,23 @@ __global__ void k_fix_links(DevTree T) {
     }
   }
 }
+__global__ void k_fix_links(DevTree T) { fix_body(T, blockIdx.x, gridDim.x); }
 
 // Resolution pass `pass` >= 1, claim half: a pending loser whose cavity holds
 // a simplex that a winner of this round removed or repointed, or whose outer
 // neighbour a winner removed, drops out for this round; the others claim
 // again with this pass's key (smaller than every earlier key of the round).
 template <int D>
-__global__ void __launch_bounds__(128) k_reclaim(DevTree T, int pass, int adjacent) {
+__device__ __forceinline__ void reclaim_body(DevTree T, int pass, int adjacent, int bid, int nblk) {
   const int round = T.ctr->round;
-  if (blockIdx.x == 0 && threadIdx.x == 0) T.ctr->win_lo = T.ctr->nwin;  // winners of this pass start here
+  if (bid == 0 && threadIdx.x == 0) T.ctr->win_lo = T.ctr->nwin;  // winners of this pass start here
   const int sin = 2 * pass - 1, sout = 2 * pass;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nc = min(T.ctr->ncand, T.cap_cand);
   const unsigned long long pe = pass_epoch(round, pass);
-  const int nw = gridDim.x * 4;
+  const int nw = nblk * 4;
   const int nin = T.ctr->nwl[sin];
-  for (int it = blockIdx.x * 4 + wib; it < nin; it += nw) {
+  for (int it = bid * 4 + wib; it < nin; it += nw) {
     const int c = T.wl[sin & 1][it];
     const int4 info = T.cinfo[c];
     if (info.w != ST_OK) continue;
@@ -1267,13 +1293,15 @@ __global__ void __launch_bounds__(128) k_reclaim(DevTree T, int pass, int adjace
     }
   }
 }
+template <int D>
+__global__ void __launch_bounds__(128) k_reclaim(DevTree T, int pass, int adjacent) { reclaim_body<D>(T, pass, adjacent, blockIdx.x, gridDim.x); }
 
 template <int D>
-__global__ void k_relocate(DevTree T) {
+__device__ __forceinline__ void relocate_body(DevTree T, int bid, int nblk) {
   const int round = T.ctr->round;
   constexpr int NV = D + 1;
   const int par = round & 1;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (bid == 0 && threadIdx.x == 0) {
     T.ctr->ncand = 0;
     T.ctr->pool_used = 0;
   }
@@ -1283,7 +1311,7 @@ __global__ void k_relocate(DevTree T) {
   int perr = 0;
   unsigned long long walk = 0;
   const int cap = 4096;
-  for (int b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+  for (int b = bid * blockDim.x; b < n; b += nblk * blockDim.x) {
     const int i = b + threadIdx.x;
     bool keep = false;
     int4 e = make_int4(-1, -1, 0, 0);
@@ -1344,9 +1372,102 @@ __global__ void k_relocate(DevTree T) {
   if (perr) set_error(T.ctr, E_PRECISION);
   flush_tally(T.ctr, tl, 0, walk);
 }
+template <int D>
+__global__ void k_relocate(DevTree T) { relocate_body<D>(T, blockIdx.x, gridDim.x); }
+
+// ---------------------------------------------------------------------------
+// Small rounds in one launch.  While few points are active a round is a
+// latency chain of about ten short kernels; here whole rounds run in one
+// cooperative launch (every block resident) with a grid barrier between the
+// phases.  The barrier's waits are bounded: a block that waits more than about
+// a second flags an error and the launch ends, so a fault in the protocol
+// cannot hang the device.
+__device__ __forceinline__ bool grid_sync(Counters* c, int nblk) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = &c->bar_gen;
+    const unsigned g = *gen;
+    __threadfence();
+    if (atomicAdd(&c->bar_count, 1u) == (unsigned)nblk - 1) {
+      c->bar_count = 0;
+      __threadfence();
+      atomicAdd(&c->bar_gen, 1u);
+    } else {
+      long long spin = 0;
+      while (*gen == g) {
+        if (++spin > (1LL << 24)) {
+          atomicExch(&c->bar_abort, 1);
+          set_error(c, E_INTERNAL);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile int*)&c->bar_abort == 0;
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_rounds_small(DevTree T, Tuning tu, unsigned long long seed, float ratio,
+                                                      int max_active, int max_rounds) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  const int bid = blockIdx.x, nblk = gridDim.x;
+  Counters* c = T.ctr;
+  for (int r = 0; r < max_rounds; ++r) {
+    plan_body(T, ratio, bid, nblk);
+    if (!grid_sync(c, nblk)) return;
+    activate_body<D>(T, seed, bid, nblk);
+    if (!grid_sync(c, nblk)) return;
+    pick_body(T, tu.thin, bid, nblk);
+    if (!grid_sync(c, nblk)) return;
+    thin_body<D>(T, tu.thin, bid, nblk);
+    if (!grid_sync(c, nblk)) return;
+    cavity_body<D>(T, tu.adjacent, bid, nblk, reinterpret_cast<WarpCav<D>*>(dsm));
+    if (!grid_sync(c, nblk)) return;
+    for (int p = 0; p < tu.passes; ++p) {
+      const int last = p == tu.passes - 1;
+      if (p > 0) {
+        reclaim_body<D>(T, p, tu.adjacent, bid, nblk);
+        if (!grid_sync(c, nblk)) return;
+      }
+      if (tu.adjacent) {
+        check_body<D, 1>(T, p, last, seed, bid, nblk, dsm);
+        if (!grid_sync(c, nblk)) return;
+        check_body<D, 2>(T, p, last, seed, bid, nblk, dsm);
+      } else {
+        check_body<D, 0>(T, p, last, seed, bid, nblk, dsm);
+      }
+      if (!grid_sync(c, nblk)) return;
+    }
+    if (tu.adjacent) {
+      fix_body(T, bid, nblk);
+      if (!grid_sync(c, nblk)) return;
+    }
+    relocate_body<D>(T, bid, nblk);
+    if (!grid_sync(c, nblk)) return;
+    if (bid == 0 && threadIdx.x == 0) {
+      const int next = c->nact[(c->round & 1) ^ 1];
+      const bool done = c->lev_next >= c->nlev && next == 0;
+      const bool grow = c->simp_overflow || c->pool_overflow || c->overflow ||
+                        (double)c->nsimp > 0.85 * (double)T.cap_simp;
+      c->coop_go = (!done && !grow && c->err == 0 && next < max_active) ? 1 : 0;
+    }
+    if (!grid_sync(c, nblk)) return;
+    if (*(volatile int*)&c->coop_go == 0) return;
+  }
+}
+
+template <int D>
+constexpr size_t small_rounds_smem() {
+  return 4 * sizeof(WarpCav<D>) > 4 * sizeof(WarpCommit<D>) ? 4 * sizeof(WarpCav<D>) : 4 * sizeof(WarpCommit<D>);
+}
 
 // Resident blocks of k_check<2>, k_check<3> on the whole GPU.
 int g_check_wave[2] = {1 << 20, 1 << 20};
+// Grid of the small-round kernel (0: not available).
+int g_small_grid[2] = {0, 0};
 
 template <int D>
 void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed& fd, Prof* pf) {
@@ -1361,7 +1482,7 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
   k_plan<<<1, 32, 0, L.stream>>>(T, fd.ratio);
   k_activate<D><<<L.blocks, 256, 0, L.stream>>>(T, fd.seed);
   mark(KT_ACTIVATE);
-  k_pick<<<L.blocks, 256, 0, L.stream>>>(T);
+  k_pick<<<L.blocks, 256, 0, L.stream>>>(T, tu.thin);
   mark(KT_PICK);
   k_thin<D><<<L.blocks, 256, 0, L.stream>>>(T, tu.thin);
   mark(KT_THIN);
@@ -1435,6 +1556,21 @@ int prepare_once() {
     return E_CUDA;
   g_check_wave[1] = std::max(1, sms * b3);
   g_check_wave[0] = std::max(1, sms * b2);
+  // small-round kernel: one block per SM when a block fits
+  int s3 = 0, s2 = 0;
+  cudaFuncSetAttribute((const void*)k_rounds_small<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)small_rounds_smem<3>());
+  cudaFuncSetAttribute((const void*)k_rounds_small<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)small_rounds_smem<2>());
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s3, k_rounds_small<3>, 128, small_rounds_smem<3>()) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s2, k_rounds_small<2>, 128, small_rounds_smem<2>()) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    s3 = s2 = 0;
+  }
+  g_small_grid[1] = s3 > 0 ? sms : 0;
+  g_small_grid[0] = s2 > 0 ? sms : 0;
   return E_OK;
 }
 }  // namespace
@@ -1447,6 +1583,26 @@ int prepare_round_kernels() {
   return rc;
 }
 
+int launch_small_rounds(const DevTree& T, cudaStream_t stream, int dim, const Tuning& tu, const Feed& fd,
+                        int max_active, int max_rounds) {
+  const int grid = g_small_grid[dim - 2];
+  if (grid <= 0) return E_CUDA;
+  DevTree t = T;
+  Tuning tuc = tu;
+  unsigned long long seed = fd.seed;
+  float ratio = fd.ratio;
+  void* args[] = {&t, &tuc, &seed, &ratio, &max_active, &max_rounds};
+  const void* fn = dim == 3 ? (const void*)k_rounds_small<3> : (const void*)k_rounds_small<2>;
+  const size_t smem = dim == 3 ? small_rounds_smem<3>() : small_rounds_smem<2>();
+  const cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(128), args, smem, stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return E_CUDA;
+  }
+  note_launches(1);
+  return E_OK;
+}
+
 void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, const Feed& fd, Prof* pf) {
   if (dim == 3)
     round_impl<3>(T, L, tu, fd, pf);
@@ -1456,6 +1612,6 @@ void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, 
 
 const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_thin",     "k_cavity", "k_check",
                                                 "k_reclaim",  "k_relocate", "k_activate", "edges",
-                                                "k_decide",   "k_fix_links"};
+                                                "k_decide",   "k_fix_links", "k_rounds_small"};
 
 }  // namespace vd

@@ -194,6 +194,14 @@ struct vd_tree {
   // warps per SM for candidate-per-warp kernels (see vd_autotune_batch)
   int blocks_per_sm = 8;
   int warps_per_sm = 20;
+  // rounds run in one cooperative launch while fewer points are active
+  int small_rounds_max = 0;
+  // early phase: until `early_until` points are inserted, rounds use thinning
+  // radius `early_thin` and feed ratio `early_ratio` (the device is mostly
+  // idle then, so extra searches are nearly free and fewer rounds pay off)
+  int64_t early_until = 10000;
+  int early_thin = 0;
+  double early_ratio = 0.5;
 };
 
 namespace {
@@ -744,26 +752,49 @@ bool launch_chunk_graph(vd_tree* t, const vd::Launch& L, int chunk, const vd::Fe
 // chunks of rounds (to grow pools and to stop); within a chunk the feed is
 // decided on the device.
 int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
-  const vd::Feed fd{seed, (float)t->ratio};
+  const vd::Feed fd_main{seed, (float)t->ratio};
+  const vd::Feed fd_early{seed, (float)std::max(t->ratio, t->early_ratio)};
+  const vd::Tuning tu_main = t->tuning;
+  vd::Tuning tu_early = t->tuning;
+  tu_early.thin = t->early_thin;
   int chunk = 1;
   int64_t last_progress = -1;
   int stalled = 0;
   int rc = vd::E_OK;
   Counters& h = *t->hctr;
   int64_t active = 0, fed = 0, done = t->hctr->ninserted;
+  // the first rounds, while few points are active, run in one cooperative
+  // launch (k_rounds_small); the rest as chunks of captured rounds
+  bool small = t->small_rounds_max > 0 && !t->trace;
   while (true) {
     if (t->trace) chunk = 1;
-    // grid sized for the most points that can be active during the chunk
-    const double grow = std::pow(1.4, chunk);
-    const int64_t est = std::min<int64_t>(n_call - fed + active,
-                                          (int64_t)((double)(done + active + 256) * grow));
-    const vd::Launch L = sized_launch(t, est);
-    if (!launch_chunk_graph(t, L, chunk, fd))
-      for (int k = 0; k < chunk; ++k) vd::launch_round(t->T, L, t->dim, t->tuning, fd, round_prof(t, k));
-    r += chunk;
+    // early phase or main phase for this chunk (the host knows the inserted count)
+    const bool early = done < t->early_until;
+    const vd::Feed& fd = early ? fd_early : fd_main;
+    t->tuning = early ? tu_early : tu_main;
+    bool ran_small = false;
+    if (small) {
+      small = false;
+      ScopedProf sp(t, vd::KT_SMALL);
+      ran_small = vd::launch_small_rounds(t->T, t->stream, t->dim, t->tuning, fd, t->small_rounds_max, 1 << 20) ==
+                  vd::E_OK;
+    }
+    if (!ran_small) {
+      // grid sized for the most points that can be active during the chunk
+      const double grow = std::pow(1.4, chunk);
+      const int64_t est = std::min<int64_t>(n_call - fed + active,
+                                            (int64_t)((double)(done + active + 256) * grow));
+      const vd::Launch L = sized_launch(t, est);
+      if (!launch_chunk_graph(t, L, chunk, fd))
+        for (int k = 0; k < chunk; ++k) vd::launch_round(t->T, L, t->dim, t->tuning, fd, round_prof(t, k));
+      r += chunk;
+    }
     rc = sync_counters(t);
     if (rc) break;
-    accumulate_events(t, chunk);
+    if (ran_small)
+      r = h.round + 1;  // the kernel decided how many rounds it ran
+    else
+      accumulate_events(t, chunk);
     if (t->trace) {
       // GPU time of the round in microseconds when profiling is on
       int64_t us = -1;
@@ -827,6 +858,7 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
     // once everything is fed the active set drains in a few rounds
     chunk = all_fed ? 2 : std::min(chunk * 2, kChunkMax);
   }
+  t->tuning = tu_main;
   return rc;
 }
 
@@ -1406,9 +1438,23 @@ int vd_set_schedule(vd_tree* t, int64_t first_prefix, double growth, double rati
 }
 
 int vd_set_tuning(vd_tree* t, int passes, int thin) {
-  if (ready(t) || passes < 1 || passes > vd::kPassesMax || thin < 1 || thin > 2) return VD_ERR_ARG;
+  if (ready(t) || passes < 1 || passes > vd::kPassesMax || thin < 0 || thin > 2) return VD_ERR_ARG;
   t->tuning.passes = passes;
   t->tuning.thin = thin;
+  return VD_OK;
+}
+
+int vd_set_early_phase(vd_tree* t, int64_t until_inserted, int thin, double ratio) {
+  if (ready(t) || until_inserted < 0 || thin < 0 || thin > 2 || !(ratio > 0.0 && ratio <= 64.0)) return VD_ERR_ARG;
+  t->early_until = until_inserted;
+  t->early_thin = thin;
+  t->early_ratio = ratio;
+  return VD_OK;
+}
+
+int vd_set_small_rounds(vd_tree* t, int max_active) {
+  if (ready(t) || max_active < 0) return VD_ERR_ARG;
+  t->small_rounds_max = max_active;
   return VD_OK;
 }
 
@@ -1587,7 +1633,7 @@ int vd_autotune_batch(vd_tree* t, const double* d_pts, const int64_t* offsets, i
   const int wps_c[] = {8, 12, 16, 20, 24, 28, 32};
   const int bps_c[] = {4, 8, 16};
   const int pass_c[] = {1, 2, 3};
-  const int thin_c[] = {1, 2};
+  const int thin_c[] = {0, 1, 2};
   const double ratio_c[] = {0.06, 0.12, 0.25, 0.5};
   const int adj_c[] = {0, 1};
   auto sweep = [&](auto field, const auto& values) {

@@ -93,6 +93,9 @@ struct Counters {
   int feed_lo, feed_hi;             // range of `order` activated this round
   int round;                        // round being run (advanced by k_plan)
   int nwin, win_lo;                 // winners of the round (adjacent mode), first of the pass
+  // grid barrier and loop decision of the small-round kernel
+  unsigned bar_count, bar_gen;
+  int bar_abort, coop_go;
 };
 
 // Points of one insertion call are split into priority levels of
@@ -252,6 +255,7 @@ enum {
   KT_EDGES,
   KT_DECIDE,
   KT_FIX,
+  KT_SMALL,
   KT_COUNT
 };
 extern const char* const kKernelTypeNames[KT_COUNT];
@@ -270,6 +274,13 @@ int prepare_round_kernels();
 // advanced by the round's first kernel), so a captured sequence of rounds
 // can be replayed.
 void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, const Feed& fd, Prof* pf);
+// Rounds while few points are active, in one cooperative launch (all blocks
+// resident, grid barrier between phases): runs until the next round's active
+// set reaches `max_active`, the call is done, `max_rounds` rounds ran, a pool
+// overflowed or an error is flagged.  Returns E_CUDA if the launch is refused
+// (then nothing ran).
+int launch_small_rounds(const DevTree& T, cudaStream_t stream, int dim, const Tuning& tu, const Feed& fd,
+                        int max_active, int max_rounds);
 
 // Edges: counts / offsets / segment buffers are caller-provided device arrays.
 struct EdgeScratch {

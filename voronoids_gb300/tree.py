@@ -286,6 +286,15 @@ class DelaunayTree:
         """Round mode: 1 lets touching cavities win together (see vd_set_adjacent)."""
         _check(_native.load().vd_set_adjacent(self._h, int(on)), "set_adjacent")
 
+    def set_early_phase(self, until_inserted=0, thin=0, ratio=0.5):
+        """Rounds of the early phase (fewer than `until_inserted` points in): thinning radius and feed ratio."""
+        _check(_native.load().vd_set_early_phase(self._h, int(until_inserted), int(thin), float(ratio)),
+               "set_early_phase")
+
+    def set_small_rounds(self, max_active=16384):
+        """Run rounds in one cooperative launch while fewer points are active (0: never)."""
+        _check(_native.load().vd_set_small_rounds(self._h, int(max_active)), "set_small_rounds")
+
     def set_graphs(self, on=True):
         _check(_native.load().vd_set_graphs(self._h, int(on)), "set_graphs")
 
