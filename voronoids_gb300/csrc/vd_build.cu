@@ -799,8 +799,8 @@ __device__ __forceinline__ void cand_lists(const DevTree& T, const int4& info, i
 template <int D>
 struct WarpCommit {
   // ridge table slots: a star of f facets has f D / 2 ridges, at most 288
-  // (3D, 192 facets) or 96 (2D, 96 facets): load factor <= 0.75
-  static constexpr int HR = D == 3 ? 512 : 128;
+  // (3D, 192 facets) or 96 (2D, 96 facets): load factor <= 0.56 / 0.375
+  static constexpr int HR = D == 3 ? 512 : 256;
   unsigned long long rk[HR];   // ridge key (r0 << 32 | r1)
   int ra[HR], rb[HR];          // the two half-ridges (facet << 2 | face)
   int id[Cap<D>::MAXF];
