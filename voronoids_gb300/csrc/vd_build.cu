@@ -829,7 +829,8 @@ __device__ __forceinline__ void ridge_of(const int* r, int g, int qf, int& r0, i
 
 // Writes one new simplex and repoints its outer neighbour.  An outer
 // neighbour that another winner of this round removed (adjacent mode) is left
-// alone: the two new simplices on that facet are linked by k_fix_links.
+// alone: the two new simplices on that facet are linked at the start of
+// k_relocate (fix_body).
 __device__ __forceinline__ void emit_simplex(const DevTree& T, const int* r, int myid, int4 nn, int round) {
   const int4 v = make_int4(r[0], r[1], r[2], r[3]);
   const int qf = r[5] & 3, o = r[4];
@@ -1005,7 +1006,7 @@ __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, i
 // Delaunay and inserting both equals inserting them one after the other.
 // MODE 1 decides (claims, facet tests, fresh slots, kill marks) for all
 // candidates of the pass, so that MODE 2, which writes the stars, knows every
-// simplex removed in the pass and leaves links into them to k_fix_links.
+// simplex removed in the pass and leaves links into them to fix_body.
 template <int D, int MODE>
 __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsigned long long seed, int bid, int nblk,
                                            unsigned char* dsm) {
@@ -1179,7 +1180,7 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
     }
     if (MODE == 2) {
       // facets shared with another winner's cavity: publish this side's new
-      // simplex and remember where the other side's goes (k_fix_links)
+      // simplex and remember where the other side's goes (fix_body)
       __syncwarp();
       for (int j = lane; j < nfac; j += 32) {
         const int o = F[6 * j + 4];
@@ -1249,7 +1250,6 @@ __device__ __forceinline__ void fix_body(DevTree T, int bid, int nblk) {
     }
   }
 }
-__global__ void k_fix_links(DevTree T) { fix_body(T, blockIdx.x, gridDim.x); }
 
 // Resolution pass `pass` >= 1, claim half: a pending loser whose cavity holds
 // a simplex that a winner of this round removed or repointed, or whose outer
@@ -1298,6 +1298,9 @@ __global__ void __launch_bounds__(128) k_reclaim(DevTree T, int pass, int adjace
 
 template <int D>
 __device__ __forceinline__ void relocate_body(DevTree T, int bid, int nblk) {
+  // adjacent mode: first link the stars of winners that share facets (the
+  // walks below stay inside stars, so they do not need those links)
+  fix_body(T, bid, nblk);
   const int round = T.ctr->round;
   constexpr int NV = D + 1;
   const int par = round & 1;
@@ -1441,10 +1444,6 @@ __global__ void __launch_bounds__(128) k_rounds_small(DevTree T, Tuning tu, unsi
       }
       if (!grid_sync(c, nblk)) return;
     }
-    if (tu.adjacent) {
-      fix_body(T, bid, nblk);
-      if (!grid_sync(c, nblk)) return;
-    }
     relocate_body<D>(T, bid, nblk);
     if (!grid_sync(c, nblk)) return;
     if (bid == 0 && threadIdx.x == 0) {
@@ -1478,7 +1477,7 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
     }
   };
   if (pf && pf->n == 0) cudaEventRecord(pf->ev[0], L.stream);
-  note_launches(tu.adjacent ? 7 + 3 * tu.passes - 1 : 6 + 2 * tu.passes - 1);
+  note_launches(tu.adjacent ? 6 + 3 * tu.passes - 1 : 6 + 2 * tu.passes - 1);
   k_plan<<<1, 32, 0, L.stream>>>(T, fd.ratio);
   k_activate<D><<<L.blocks, 256, 0, L.stream>>>(T, fd.seed);
   mark(KT_ACTIVATE);
@@ -1503,10 +1502,6 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
       k_check<D, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
     }
     mark(KT_CHECK);
-  }
-  if (tu.adjacent) {
-    k_fix_links<<<L.warps / 4, 128, 0, L.stream>>>(T);
-    mark(KT_FIX);
   }
   k_relocate<D><<<L.blocks, 256, 0, L.stream>>>(T);
   mark(KT_RELOCATE);
