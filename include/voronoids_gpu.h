@@ -70,6 +70,7 @@ typedef struct vd_stats {
   int64_t searched;          /* nominations that won the thinning claim and were searched */
   int64_t won_pass[3];       /* insertions decided in resolution pass 0, 1, 2 and later */
   int64_t spilled;           /* cavity searches that spilled to the pool */
+  int64_t max_search_levels; /* deepest conflict-region search (breadth-first levels) */
 } vd_stats;
 
 /* DelaunayTree::<3,4>::new / ::<2,3>::new
@@ -200,6 +201,19 @@ int vd_set_small_rounds(vd_tree* t, int max_active);
  * points, radius 0, ratio 0.5; until_inserted = 0 turns it off.  No
  * reference counterpart; the triangulation is the same. */
 int vd_set_early_phase(vd_tree* t, int64_t until_inserted, int thin, double ratio);
+/* Exact tier of the conflict tests (the insphere sign when the FP32 and FP64
+ * filters cannot decide).  mode 1: floating-point expansions only; mode 2:
+ * an integer evaluation first (every coordinate a multiple of a common power
+ * of two within 126 bits, 32-bit limbs), the expansions beyond that; mode 0
+ * (default): expansions until a call has made `switch_after` exact tests
+ * (default 32), then the integer form for the rest of the call.  The kernels
+ * of each form are compiled separately: the integer form needs far more
+ * registers, which slows inputs that never reach the exact tier, while on
+ * near-degenerate inputs it is several times faster than the expansions.
+ * Every mode gives the same signs, so the same triangulation.  The
+ * reference's conflict test (circumsphere centre and radius, then a distance
+ * comparison in f64, src/geometry.rs:58-97) has no exact tier. */
+int vd_set_exact_tier(vd_tree* t, int mode, int64_t switch_after);
 /* Rounds are launched in chunks captured once as CUDA graphs and replayed
  * (default on; profiling and tracing launch kernel by kernel).  No reference
  * counterpart. */

@@ -16,6 +16,7 @@ def host():
     H = ctypes.CDLL(B.build_host())
     H.vdh_in_conflict.argtypes = [ctypes.c_int, dp, ip, ip, ip]
     H.vdh_insphere_exact.argtypes = [ctypes.c_int, dp, ip, ctypes.c_int, ip]
+    H.vdh_insphere_exact_expansion.argtypes = [ctypes.c_int, dp, ip, ctypes.c_int, ip]
     H.vdh_orient_exact.argtypes = [ctypes.c_int, dp, ip]
     H.vdh_exit_face.argtypes = [ctypes.c_int, dp, ctypes.c_uint, ctypes.c_int, ip]
     return H
@@ -179,3 +180,50 @@ def test_split_exit_face(host, oracle, dim):
                     want = j
                     break
             assert got == want
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_exact_tier_integer_and_expansion_paths(host, oracle, dim):
+    # The exact tier works on integers when every coordinate is a multiple of
+    # a common power of two within 126 bits, and on floating-point expansions
+    # otherwise.  Near-cospherical lattices, exact ties (perturbation), small
+    # and huge coordinates mixed (beyond the integer budget) all against the
+    # oracle's big integers.
+    rng = np.random.default_rng(900 + dim)
+    checked = 0
+    for trial in range(4000):
+        kind = trial % 5
+        if kind == 0:  # jittered lattice (near-degenerate, integer path)
+            pts = np.round(rng.random((dim + 2, dim)) * 64) / 64 + rng.uniform(-1e-12, 1e-12, (dim + 2, dim))
+        elif kind == 1:  # exact lattice (ties: perturbation on exact minors)
+            pts = np.round(rng.random((dim + 2, dim)) * 6) / 6
+        elif kind == 2:  # super-simplex scale next to unit-cube points
+            pts = rng.random((dim + 2, dim))
+            pts[0] = pts[0] * 40 - 20
+        elif kind == 3:  # exponents spread wider than 126 bits: expansion path
+            pts = rng.random((dim + 2, dim))
+            pts[1, 0] = 1e-30 + pts[1, 0] * 1e-31
+            pts[2, 0] = 3.0e9
+        else:  # tiny query offsets from a vertex
+            pts = rng.random((dim + 2, dim))
+            pts[-1] = pts[1] + rng.uniform(-1e-14, 1e-14, dim)
+        s = pts[: dim + 1]
+        o = oracle.orient(s)
+        if o == 0:
+            continue
+        if o < 0:
+            s = s[[1, 0] + list(range(2, dim + 1))]
+        pts = np.vstack([s, pts[dim + 1:]])
+        keys = np.ascontiguousarray(rng.permutation(64)[: dim + 2], dtype=np.int32)
+        P = _pad(pts, dim)
+        err = ctypes.c_int()
+        want_g = oracle.insphere_sos(pts[: dim + 1], pts[dim + 1], keys)
+        want_u = oracle.insphere_exact(pts[: dim + 1], pts[dim + 1])
+        for fn in (host.vdh_insphere_exact, host.vdh_insphere_exact_expansion):
+            g = fn(dim, P.ctypes.data_as(dp), keys.ctypes.data_as(ip), 1, ctypes.byref(err))
+            u = fn(dim, P.ctypes.data_as(dp), keys.ctypes.data_as(ip), 0, ctypes.byref(err))
+            assert err.value == 0
+            assert g == want_g, (fn.__name__, kind, pts.tolist(), keys.tolist())
+            assert u == want_u, (fn.__name__, kind, pts.tolist())
+        checked += 1
+    assert checked > 3500

@@ -498,7 +498,7 @@ struct WarpCtl {
 // Breadth-first search of the conflict region of candidate q from the
 // simplex that contains it; all 32 lanes of the warp call this.  Returns
 // with ctl.flags != 0 if a capacity was exceeded.
-template <int D>
+template <int D, int XT>
 __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl, int lane, int start,
                               int4 v0, int4 n0, int qv, const vdp::VPt& q, const vdp::FPt& fq,
                               vdp::Tally& tl, int& perr, unsigned long long& ntests) {
@@ -515,10 +515,11 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
   __syncwarp();
   if (lane == 0) hset_insert(S.hk, S.hs, start);
   __syncwarp();
-  int head = 0;
+  int head = 0, levels = 0;
   while (true) {
     const int hi = min(*(volatile int*)&ctl.ncav, S.maxc);
     if (*(volatile int*)&ctl.flags || head >= hi) break;
+    ++levels;
     const int items = (hi - head) * NV;
     for (int it = lane; it < items; it += 32) {
       const int k = head + it / NV, f = it - (it / NV) * NV;
@@ -544,7 +545,7 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
             for (int j = 0; j < NV; ++j) v64[j] = load_pt(T, kv[j]);
             q64 = q;
           };
-          if (vdp::in_conflict_hl<D>(fv, kv, fq, qv, tl, perr, load64)) {
+          if (vdp::in_conflict_hl<D, XT>(fv, kv, fq, qv, tl, perr, load64)) {
             if (hset_insert(S.hk, S.hs, nb)) {
               int s = atomicAdd(&ctl.ncav, 1);
               if (s < S.maxc) {
@@ -580,6 +581,7 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
     head = hi;
   }
   __syncwarp();
+  if (lane == 0 && levels > 64) atomicMax(&T.ctr->max_levels, levels);
 }
 
 // Thinning test of one nominee (one thread): it must hold the thinning claim
@@ -673,7 +675,7 @@ __device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int
   }
 }
 
-template <int D>
+template <int D, int XT>
 __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, int nblk, WarpCav<D>* smem) {
   const int round = T.ctr->round;
   constexpr int MAXC = Cap<D>::MAXC, MAXF = Cap<D>::MAXF, HS = Cap<D>::HS;
@@ -700,7 +702,7 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
     load_simplex(T, cd.y, v0, n0);
     if (lane == 0) ++nsearched;
     const unsigned long long key = pe | (unsigned)cd.z;
-    cavity_search<D>(T, fast, W.ctl, lane, cd.y, v0, n0, cd.x, q, fq, tl, perr, ntests);
+    cavity_search<D, XT>(T, fast, W.ctl, lane, cd.y, v0, n0, cd.x, q, fq, tl, perr, ntests);
     int ncav = min(W.ctl.ncav, MAXC), nfac = min(W.ctl.nfac, MAXF);
     int off = 0;
     if (W.ctl.flags) {
@@ -721,7 +723,7 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
       int* P = T.pool + off;
       const CavStore big{P, reinterpret_cast<int4*>(P + kOffCV), reinterpret_cast<int4*>(P + kOffCN),
                          P + kOffH, P + kOffF, kBigC, kBigF, kBigH};
-      cavity_search<D>(T, big, W.ctl, lane, cd.y, v0, n0, cd.x, q, fq, tl, perr, ntests);
+      cavity_search<D, XT>(T, big, W.ctl, lane, cd.y, v0, n0, cd.x, q, fq, tl, perr, ntests);
       if (W.ctl.flags) {
         if (lane == 0) {
           T.cinfo[c] = make_int4(W.ctl.ncav, W.ctl.nfac, 0, ST_OVERFLOW);
@@ -780,9 +782,9 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
     if (mfac) atomicMax(&T.ctr->max_fac, mfac);
   }
 }
-template <int D>
+template <int D, int XT>
 __global__ void __launch_bounds__(128, VD_CAVITY_MIN_BLOCKS) k_cavity(DevTree T, int adjacent) { __shared__ WarpCav<D> smem[4];
-  cavity_body<D>(T, adjacent, blockIdx.x, gridDim.x, smem); }
+  cavity_body<D, XT>(T, adjacent, blockIdx.x, gridDim.x, smem); }
 
 // Pool layout of a searched candidate: cavity ids at P, facet records at
 // P + ncav, or at P + kOffF for a spilled (large) search, flagged by bit 30
@@ -1007,7 +1009,7 @@ __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, i
 // MODE 1 decides (claims, facet tests, fresh slots, kill marks) for all
 // candidates of the pass, so that MODE 2, which writes the stars, knows every
 // simplex removed in the pass and leaves links into them to fix_body.
-template <int D, int MODE>
+template <int D, int MODE, int XT>
 __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsigned long long seed, int bid, int nblk,
                                            unsigned char* dsm) {
   constexpr int NV = D + 1;
@@ -1073,7 +1075,7 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
             for (int i = 0; i < NV; ++i) v64[i] = load_pt(T, r[i]);
             p64 = load_pt(T, xv);
           };
-          ok = !vdp::in_conflict_hl<D>(fv, r, fx, xv, tl, perr, load64);
+          ok = !vdp::in_conflict_hl<D, XT>(fv, r, fx, xv, tl, perr, load64);
         }
       }
       if (!__all_sync(FULL, ok)) {
@@ -1220,9 +1222,9 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
     }
   }
 }
-template <int D, int MODE>
+template <int D, int MODE, int XT>
 __global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last, unsigned long long seed) { extern __shared__ __align__(16) unsigned char dsm[];
-  check_body<D, MODE>(T, pass, last, seed, blockIdx.x, gridDim.x, dsm); }
+  check_body<D, MODE, XT>(T, pass, last, seed, blockIdx.x, gridDim.x, dsm); }
 
 // Adjacent mode, end of a round: a new simplex whose outer neighbour another
 // winner removed takes, as that neighbour, the other winner's new simplex on
@@ -1427,7 +1429,7 @@ __global__ void __launch_bounds__(128) k_rounds_small(DevTree T, Tuning tu, unsi
     if (!grid_sync(c, nblk)) return;
     thin_body<D>(T, tu.thin, bid, nblk);
     if (!grid_sync(c, nblk)) return;
-    cavity_body<D>(T, tu.adjacent, bid, nblk, reinterpret_cast<WarpCav<D>*>(dsm));
+    cavity_body<D, 0>(T, tu.adjacent, bid, nblk, reinterpret_cast<WarpCav<D>*>(dsm));
     if (!grid_sync(c, nblk)) return;
     for (int p = 0; p < tu.passes; ++p) {
       const int last = p == tu.passes - 1;
@@ -1436,11 +1438,11 @@ __global__ void __launch_bounds__(128) k_rounds_small(DevTree T, Tuning tu, unsi
         if (!grid_sync(c, nblk)) return;
       }
       if (tu.adjacent) {
-        check_body<D, 1>(T, p, last, seed, bid, nblk, dsm);
+        check_body<D, 1, 0>(T, p, last, seed, bid, nblk, dsm);
         if (!grid_sync(c, nblk)) return;
-        check_body<D, 2>(T, p, last, seed, bid, nblk, dsm);
+        check_body<D, 2, 0>(T, p, last, seed, bid, nblk, dsm);
       } else {
-        check_body<D, 0>(T, p, last, seed, bid, nblk, dsm);
+        check_body<D, 0, 0>(T, p, last, seed, bid, nblk, dsm);
       }
       if (!grid_sync(c, nblk)) return;
     }
@@ -1485,7 +1487,12 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
   mark(KT_PICK);
   k_thin<D><<<L.blocks, 256, 0, L.stream>>>(T, tu.thin);
   mark(KT_THIN);
-  k_cavity<D><<<L.warps / 4, 128, 0, L.stream>>>(T, tu.adjacent);
+  // kernels with conflict tests come in two forms: exact tier on expansions
+  // alone (small register allocation) or integer tier first (tu.exact_int)
+  if (tu.exact_int)
+    k_cavity<D, 1><<<L.warps / 4, 128, 0, L.stream>>>(T, tu.adjacent);
+  else
+    k_cavity<D, 0><<<L.warps / 4, 128, 0, L.stream>>>(T, tu.adjacent);
   mark(KT_CAVITY);
   const int commit_grid = std::min(L.warps / 4, g_check_wave[D - 2]);
   for (int p = 0; p < tu.passes; ++p) {
@@ -1495,11 +1502,16 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
       mark(KT_RECLAIM);
     }
     if (tu.adjacent) {
-      k_check<D, 1><<<L.warps / 4, 128, 0, L.stream>>>(T, p, last, fd.seed);
+      if (tu.exact_int)
+        k_check<D, 1, 1><<<L.warps / 4, 128, 0, L.stream>>>(T, p, last, fd.seed);
+      else
+        k_check<D, 1, 0><<<L.warps / 4, 128, 0, L.stream>>>(T, p, last, fd.seed);
       mark(KT_DECIDE);
-      k_check<D, 2><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
+      k_check<D, 2, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
+    } else if (tu.exact_int) {
+      k_check<D, 0, 1><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
     } else {
-      k_check<D, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
+      k_check<D, 0, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
     }
     mark(KT_CHECK);
   }
@@ -1537,17 +1549,19 @@ int prepare_once() {
     const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (r != cudaSuccess) e = r;
   };
-  attr((const void*)k_check<3, 0>, 4 * (int)sizeof(WarpCommit<3>));
-  attr((const void*)k_check<3, 2>, 4 * (int)sizeof(WarpCommit<3>));
-  attr((const void*)k_check<2, 0>, 4 * (int)sizeof(WarpCommit<2>));
-  attr((const void*)k_check<2, 2>, 4 * (int)sizeof(WarpCommit<2>));
+  attr((const void*)k_check<3, 0, 0>, 4 * (int)sizeof(WarpCommit<3>));
+  attr((const void*)k_check<3, 0, 1>, 4 * (int)sizeof(WarpCommit<3>));
+  attr((const void*)k_check<3, 2, 0>, 4 * (int)sizeof(WarpCommit<3>));
+  attr((const void*)k_check<2, 0, 0>, 4 * (int)sizeof(WarpCommit<2>));
+  attr((const void*)k_check<2, 0, 1>, 4 * (int)sizeof(WarpCommit<2>));
+  attr((const void*)k_check<2, 2, 0>, 4 * (int)sizeof(WarpCommit<2>));
   if (e != cudaSuccess) return E_CUDA;
   // k_check is a grid-stride loop: one resident wave avoids a ragged second
   int dev = 0, sms = 0, b3 = 0, b2 = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_check<3, 0>, 128, 4 * sizeof(WarpCommit<3>)) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_check<2, 0>, 128, 4 * sizeof(WarpCommit<2>)) != cudaSuccess)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_check<3, 0, 1>, 128, 4 * sizeof(WarpCommit<3>)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_check<2, 0, 1>, 128, 4 * sizeof(WarpCommit<2>)) != cudaSuccess)
     return E_CUDA;
   g_check_wave[1] = std::max(1, sms * b3);
   g_check_wave[0] = std::max(1, sms * b2);

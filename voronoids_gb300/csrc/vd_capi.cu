@@ -168,7 +168,7 @@ struct vd_tree {
   // bakes in (the device tree by value, grid, tuning and feed)
   struct ChunkGraph {
     vd::DevTree T;
-    int chunk, blocks, warps, passes, thin, adjacent;
+    int chunk, blocks, warps, passes, thin, adjacent, exact_int;
     uint64_t seed;
     float ratio;
     long long launches;
@@ -202,6 +202,11 @@ struct vd_tree {
   int64_t early_until = 10000;
   int early_thin = 0;
   double early_ratio = 0.5;
+  // exact tier of the conflict tests: 0 automatic (expansions until a build
+  // has made `exact_switch` exact tests, then the integer tier first),
+  // 1 expansions only, 2 integer tier first from the start
+  int exact_mode = 0;
+  int64_t exact_switch = 32;
 };
 
 namespace {
@@ -699,7 +704,8 @@ bool launch_chunk_graph(vd_tree* t, const vd::Launch& L, int chunk, const vd::Fe
   vd_tree::ChunkGraph* hit = nullptr;
   for (auto& g : t->graphs)
     if (g.chunk == chunk && g.blocks == L.blocks && g.warps == L.warps && g.passes == t->tuning.passes &&
-        g.thin == t->tuning.thin && g.adjacent == t->tuning.adjacent && g.seed == fd.seed && g.ratio == fd.ratio &&
+        g.thin == t->tuning.thin && g.adjacent == t->tuning.adjacent && g.exact_int == t->tuning.exact_int &&
+        g.seed == fd.seed && g.ratio == fd.ratio &&
         memcmp(&g.T, &t->T, sizeof(vd::DevTree)) == 0) {
       hit = &g;
       break;
@@ -731,6 +737,7 @@ bool launch_chunk_graph(vd_tree* t, const vd::Launch& L, int chunk, const vd::Fe
     g.passes = t->tuning.passes;
     g.thin = t->tuning.thin;
     g.adjacent = t->tuning.adjacent;
+    g.exact_int = t->tuning.exact_int;
     g.seed = fd.seed;
     g.ratio = fd.ratio;
     g.launches = launches;
@@ -763,6 +770,9 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
   int rc = vd::E_OK;
   Counters& h = *t->hctr;
   int64_t active = 0, fed = 0, done = t->hctr->ninserted;
+  // exact tests of this call so far decide the form of the conflict-test kernels
+  const unsigned long long exact0 = h.tally[2];
+  bool exact_int = t->exact_mode == 2;
   // the first rounds, while few points are active, run in one cooperative
   // launch (k_rounds_small); the rest as chunks of captured rounds
   bool small = t->small_rounds_max > 0 && !t->trace;
@@ -772,6 +782,7 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
     const bool early = done < t->early_until;
     const vd::Feed& fd = early ? fd_early : fd_main;
     t->tuning = early ? tu_early : tu_main;
+    t->tuning.exact_int = exact_int ? 1 : 0;
     bool ran_small = false;
     if (small) {
       small = false;
@@ -817,6 +828,7 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
       rc = h.err;
       break;
     }
+    if (t->exact_mode == 0 && (int64_t)(h.tally[2] - exact0) >= t->exact_switch) exact_int = true;
     active = h.nact[r & 1];
     fed = h.feed_hi;
     done = h.ninserted;
@@ -1377,6 +1389,7 @@ int vd_get_stats(vd_tree* t, vd_stats* s) {
   for (int p = 0; p < 3; ++p) s->won_pass[p] = (int64_t)h.won[p];
   for (int p = 3; p < vd::kPassesMax; ++p) s->won_pass[2] += (int64_t)h.won[p];
   s->spilled = (int64_t)h.spilled;
+  s->max_search_levels = h.max_levels;
   return VD_OK;
 }
 
@@ -1449,6 +1462,13 @@ int vd_set_early_phase(vd_tree* t, int64_t until_inserted, int thin, double rati
   t->early_until = until_inserted;
   t->early_thin = thin;
   t->early_ratio = ratio;
+  return VD_OK;
+}
+
+int vd_set_exact_tier(vd_tree* t, int mode, int64_t switch_after) {
+  if (ready(t) || mode < 0 || mode > 2 || switch_after < 0) return VD_ERR_ARG;
+  t->exact_mode = mode;
+  t->exact_switch = switch_after;
   return VD_OK;
 }
 

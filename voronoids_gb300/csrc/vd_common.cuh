@@ -93,6 +93,7 @@ struct Counters {
   int feed_lo, feed_hi;             // range of `order` activated this round
   int round;                        // round being run (advanced by k_plan)
   int nwin, win_lo;                 // winners of the round (adjacent mode), first of the pass
+  int max_levels;                   // deepest cavity search (breadth-first levels)
   // grid barrier and loop decision of the small-round kernel
   unsigned bar_count, bar_gen;
   int bar_abort, coop_go;
@@ -242,6 +243,7 @@ struct Tuning {
   int passes;
   int thin;
   int adjacent;  // 1: cavities of one pass may touch (see k_check in vd_build.cu)
+  int exact_int;  // 1: conflict tests use the integer exact tier before the expansions
 };
 // Kernel types for profiling.
 enum {

@@ -26,7 +26,8 @@ int vdh_in_conflict(int dim, const double* pts, const int* keys, int* tier_out, 
   return c ? 1 : -1;
 }
 
-// Exact expansion-arithmetic tier only (perturbed when sos != 0).
+// Exact tier only (perturbed when sos != 0): the integer evaluation first,
+// then the expansions.
 int vdh_insphere_exact(int dim, const double* pts, const int* keys, int sos, int* err_out) {
   vdp::VPt p[4];
   for (int i = 0; i <= dim; ++i) p[i] = at(pts, i);
@@ -34,6 +35,19 @@ int vdh_insphere_exact(int dim, const double* pts, const int* keys, int sos, int
   int err = 0;
   int s = dim == 3 ? vdp::exact_insphere_sos<3>(p, keys, q, keys[dim + 1], err, sos != 0)
                    : vdp::exact_insphere_sos<2>(p, keys, q, keys[dim + 1], err, sos != 0);
+  if (err_out) *err_out = err;
+  return s;
+}
+
+// The expansion form of the exact tier alone (the form of kernels that keep
+// their register allocation small).
+int vdh_insphere_exact_expansion(int dim, const double* pts, const int* keys, int sos, int* err_out) {
+  vdp::VPt p[4];
+  for (int i = 0; i <= dim; ++i) p[i] = at(pts, i);
+  vdp::VPt q = at(pts, dim + 1);
+  int err = 0;
+  int s = dim == 3 ? vdp::exact_insphere_sos<3, 0>(p, keys, q, keys[dim + 1], err, sos != 0)
+                   : vdp::exact_insphere_sos<2, 0>(p, keys, q, keys[dim + 1], err, sos != 0);
   if (err_out) *err_out = err;
   return s;
 }

@@ -51,8 +51,9 @@
 // VDP_XCAP components; exceeding it sets an error flag (never a silent wrong
 // answer).
 #pragma once
-#include <stdint.h>
 #include <math.h>
+#include <stdint.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #define VDP_HD __host__ __device__ __forceinline__
@@ -325,13 +326,272 @@ VDP_HD int sos_decide(const int* s, const int* key, int qkey) {
   return -1;
 }
 
+// ---------------------------------------------------------------------------
+// Exact tier in integer arithmetic.  The FP64 pipe of this GPU is narrow
+// (a few operations per clock per SM) while 32-bit integer multiply-adds run
+// at full rate, so the lifted determinant is evaluated on integers: every
+// coordinate of the D + 2 points is m * 2^e with a 53-bit integer m (read
+// from its bit pattern); with e0 the lowest set bit among them, each one is
+// an integer multiple of 2^e0.  When all of them are below 2^(e0 + 126),
+// the rows d = p_i - q are 127-bit integers and the determinant is computed
+// exactly with 32-bit limbs (sign-magnitude, schoolbook products).  Wider
+// spreads of exponents are left to the expansion path.
+// ---------------------------------------------------------------------------
+template <int N>
+struct SInt {
+  uint32_t m[N];
+  int neg;
+};
+
+template <int N>
+VDP_HD bool sint_zero(const SInt<N>& a) {
+  uint32_t o = 0;
+  for (int i = 0; i < N; ++i) o |= a.m[i];
+  return o == 0;
+}
+template <int N>
+VDP_HD int sint_sign(const SInt<N>& a) { return sint_zero(a) ? 0 : (a.neg ? -1 : 1); }
+
+// |a| vs |b|
+template <int N>
+VDP_HD int mag_cmp(const uint32_t* a, const uint32_t* b) {
+  for (int i = N - 1; i >= 0; --i)
+    if (a[i] != b[i]) return a[i] < b[i] ? -1 : 1;
+  return 0;
+}
+
+// acc += x (signed), both N limbs; the caller sizes N so that no carry leaves
+template <int N>
+VDP_HD void sint_add(SInt<N>& acc, const SInt<N>& x) {
+  if (sint_zero(x)) return;
+  if (sint_zero(acc) || acc.neg == x.neg) {
+    if (sint_zero(acc)) acc.neg = x.neg;
+    unsigned long long c = 0;
+    for (int i = 0; i < N; ++i) {
+      c += (unsigned long long)acc.m[i] + x.m[i];
+      acc.m[i] = (uint32_t)c;
+      c >>= 32;
+    }
+    return;
+  }
+  // opposite signs: subtract the smaller magnitude from the larger
+  const uint32_t* big = acc.m;
+  const uint32_t* small = x.m;
+  int sign = acc.neg;
+  uint32_t tmp[N];
+  if (mag_cmp<N>(acc.m, x.m) < 0) {
+    for (int i = 0; i < N; ++i) tmp[i] = acc.m[i];
+    big = x.m;
+    small = tmp;
+    sign = x.neg;
+  }
+  long long br = 0;
+  uint32_t out[N];
+  for (int i = 0; i < N; ++i) {
+    long long d = (long long)big[i] - small[i] - br;
+    br = d < 0 ? 1 : 0;
+    out[i] = (uint32_t)(d + (br << 32));
+  }
+  for (int i = 0; i < N; ++i) acc.m[i] = out[i];
+  acc.neg = sign;
+}
+
+// r = a * b (signed), NA + NB limbs
+template <int NA, int NB>
+VDP_HD void sint_mul(SInt<NA + NB>& r, const SInt<NA>& a, const SInt<NB>& b) {
+  for (int i = 0; i < NA + NB; ++i) r.m[i] = 0;
+  for (int i = 0; i < NA; ++i) {
+    if (a.m[i] == 0) continue;
+    unsigned long long c = 0;
+    for (int j = 0; j < NB; ++j) {
+      c += (unsigned long long)a.m[i] * b.m[j] + r.m[i + j];
+      r.m[i + j] = (uint32_t)c;
+      c >>= 32;
+    }
+    for (int k = i + NB; c && k < NA + NB; ++k) {
+      c += r.m[k];
+      r.m[k] = (uint32_t)c;
+      c >>= 32;
+    }
+  }
+  r.neg = a.neg ^ b.neg;
+}
+
+template <int NS, int ND>
+VDP_HD void sint_widen(SInt<ND>& d, const SInt<NS>& s) {
+  for (int i = 0; i < ND; ++i) d.m[i] = i < NS ? s.m[i] : 0;
+  d.neg = s.neg;
+}
+
+VDP_HD unsigned long long dbits(double x) {
+#if defined(__CUDA_ARCH__)
+  return (unsigned long long)__double_as_longlong(x);
+#else
+  unsigned long long b;
+  memcpy(&b, &x, 8);
+  return b;
+#endif
+}
+
+// x = m * 2^e with the 53-bit integer m; false for 0, subnormals, inf, NaN.
+VDP_HD bool dsplit(double x, unsigned long long& m, int& e, int& neg) {
+  const unsigned long long b = dbits(x);
+  const int ef = (int)((b >> 52) & 0x7ff);
+  if (ef == 0 || ef == 0x7ff) return false;
+  m = (b & 0xfffffffffffffULL) | (1ULL << 52);
+  e = ef - 1075;
+  neg = (int)(b >> 63);
+  return true;
+}
+
+VDP_HD int ctz64(unsigned long long v) {
+#if defined(__CUDA_ARCH__)
+  return __ffsll((long long)v) - 1;
+#else
+  return __builtin_ctzll(v);
+#endif
+}
+
+// Integer exact lifted determinant.  Returns 2 when the exponents spread
+// too far (undecided); otherwise the sign of the determinant, and the signs
+// of the minors O_i in s[] (for the perturbation rule).
+template <int D>
+VDP_HD int insphere_int(const VPt* p, const VPt& q, int* s) {
+  constexpr int NV = D + 1;
+  constexpr int NP = NV + 1;
+  double c[NP][3];
+  for (int i = 0; i < NV; ++i) {
+    c[i][0] = p[i].x;
+    c[i][1] = p[i].y;
+    c[i][2] = p[i].z;
+  }
+  c[NV][0] = q.x;
+  c[NV][1] = q.y;
+  c[NV][2] = q.z;
+  int e0 = 1 << 30, top = -(1 << 30);
+  for (int i = 0; i < NP; ++i)
+    for (int k = 0; k < D; ++k) {
+      if (c[i][k] == 0.0) continue;
+      unsigned long long m;
+      int e, ng;
+      if (!dsplit(c[i][k], m, e, ng)) return 2;
+      const int lo = e + ctz64(m);
+      e0 = lo < e0 ? lo : e0;
+      top = e + 53 > top ? e + 53 : top;
+    }
+  if (top == -(1 << 30)) return 0;  // all coordinates zero
+  if (top - e0 > 126) return 2;
+  // coordinates as 4-limb integers (value / 2^e0)
+  SInt<4> v[NP][3];
+  for (int i = 0; i < NP; ++i)
+    for (int k = 0; k < 3; ++k) {
+      SInt<4>& z = v[i][k];
+      z.m[0] = z.m[1] = z.m[2] = z.m[3] = 0;
+      z.neg = 0;
+      if (k >= D || c[i][k] == 0.0) continue;
+      unsigned long long m;
+      int e, ng;
+      dsplit(c[i][k], m, e, ng);
+      const int tz = ctz64(m);  // drop the zero low bits: m * 2^e, m odd
+      m >>= tz;
+      e += tz;
+      const int sh = e - e0;  // 0 <= sh (e0 is the lowest set bit), m << sh < 2^126
+      const int w = sh >> 5, b = sh & 31;
+      const unsigned long long lo = m << b;
+      const unsigned long long hi = b ? (m >> (64 - b)) : 0ULL;
+      const uint32_t part[4] = {(uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32)};
+      for (int t = 0; t < 4; ++t)
+        if (w + t < 4) z.m[w + t] = part[t];
+      z.neg = ng;
+    }
+  // rows d_i = p_i - q
+  SInt<4> d[NV][3];
+  for (int i = 0; i < NV; ++i)
+    for (int k = 0; k < 3; ++k) {
+      d[i][k] = v[i][k];
+      SInt<4> nq = v[NV][k];
+      nq.neg ^= 1;
+      sint_add(d[i][k], nq);
+    }
+  SInt<D == 3 ? 21 : 17> det;
+  for (int i = 0; i < (D == 3 ? 21 : 17); ++i) det.m[i] = 0;
+  det.neg = 0;
+  for (int i = 0; i < NV; ++i) {
+    // w_i = |d_i|^2 (8 limbs)
+    SInt<8> w, t8;
+    for (int j = 0; j < 8; ++j) w.m[j] = 0;
+    w.neg = 0;
+    for (int k = 0; k < D; ++k) {
+      sint_mul<4, 4>(t8, d[i][k], d[i][k]);
+      sint_add(w, t8);
+    }
+    if constexpr (D == 3) {
+      int o[3], t = 0;
+      for (int k = 0; k < 4; ++k)
+        if (k != i) o[t++] = k;
+      // det3 rows (x, y, z) of o[0..2], expanded along z as the expansion path does
+      SInt<12> O, t12;
+      for (int j = 0; j < 12; ++j) O.m[j] = 0;
+      O.neg = 0;
+      const int pr[3][2] = {{1, 2}, {0, 2}, {0, 1}};
+      for (int r = 0; r < 3; ++r) {
+        const int a = o[pr[r][0]], b = o[pr[r][1]];
+        SInt<8> mnr, t2;
+        sint_mul<4, 4>(mnr, d[a][0], d[b][1]);
+        sint_mul<4, 4>(t2, d[a][1], d[b][0]);
+        t2.neg ^= 1;
+        sint_add(mnr, t2);
+        sint_mul<4, 8>(t12, d[o[r]][2], mnr);
+        if (r == 1) t12.neg ^= 1;
+        sint_add(O, t12);
+      }
+      if (!(i & 1)) O.neg ^= 1;  // O_i = (-1)^(i+1) det3
+      s[i] = sint_sign(O);
+      SInt<20> t20;
+      SInt<21> t21;
+      sint_mul<8, 12>(t20, w, O);
+      sint_widen(t21, t20);
+      sint_add(det, t21);
+    } else {
+      int o[2], t = 0;
+      for (int k = 0; k < 3; ++k)
+        if (k != i) o[t++] = k;
+      SInt<8> O, t2;
+      sint_mul<4, 4>(O, d[o[0]][0], d[o[1]][1]);
+      sint_mul<4, 4>(t2, d[o[0]][1], d[o[1]][0]);
+      t2.neg ^= 1;
+      sint_add(O, t2);
+      if (i & 1) O.neg ^= 1;  // O_i = (-1)^i minor
+      s[i] = sint_sign(O);
+      SInt<16> t16;
+      SInt<17> t17;
+      sint_mul<8, 8>(t16, w, O);
+      sint_widen(t17, t16);
+      sint_add(det, t17);
+    }
+  }
+  return sint_sign(det);
+}
+
 // Exact, perturbed insphere (3D) / incircle (2D).  p[i] positively oriented.
 // With sos = false the plain sign of the lifted determinant is returned
 // (0 when q is exactly on the circumsphere).
-template <int D>
+//
+// XT selects the integer tier in front of the expansions.  The integer code
+// is wide (many live limbs); a kernel whose register allocation must stay
+// small calls the XT = 0 form, which is the expansion path alone.
+template <int D, int XT = 1>
 VDP_NI int exact_insphere_sos(const VPt* p, const int* key, const VPt& q, int qkey, int& err,
                               bool sos = true) {
   constexpr int NV = D + 1;
+  if constexpr (XT != 0) {
+    int si[NV];
+    const int r = insphere_int<D>(p, q, si);
+    if (r != 2) {
+      if (r != 0 || !sos) return r;
+      return sos_decide<NV>(si, key, qkey);
+    }
+  }
   X2 x[NV], y[NV], z[NV];
   for (int k = 0; k < NV; ++k) {
     x[k] = x2_diff(p[k].x, q.x);
@@ -723,7 +983,7 @@ VDP_HD int insphere_hl(const FPt* v, const FPt& q) {
 }
 
 // The FP64 and exact tiers of in_conflict (used when the split tier is undecided).
-template <int D>
+template <int D, int XT = 1>
 VDP_HD bool in_conflict_64(const VPt* p, const int* key, const VPt& q, int qkey, Tally& t, int& err) {
   constexpr int NV = D + 1;
   double dx[NV], dy[NV], dz[NV];
@@ -742,13 +1002,13 @@ VDP_HD bool in_conflict_64(const VPt* p, const int* key, const VPt& q, int qkey,
     return s > 0;
   }
   t.exact++;
-  s = exact_insphere_sos<D>(p, key, q, qkey, err);
+  s = exact_insphere_sos<D, XT>(p, key, q, qkey, err);
   return s > 0;
 }
 
 // Tiered conflict test starting from split coordinates; load64(v, q) fills
 // the f64 coordinates when the f32 tier cannot decide.
-template <int D, class Load64>
+template <int D, int XT = 1, class Load64>
 VDP_HD bool in_conflict_hl(const FPt* fv, const int* key, const FPt& fq, int qkey, Tally& t, int& err,
                            Load64 load64) {
   const int s = insphere_hl<D>(fv, fq);
@@ -758,7 +1018,7 @@ VDP_HD bool in_conflict_hl(const FPt* fv, const int* key, const FPt& fq, int qke
   }
   VPt v[D + 1], q;
   load64(v, q);
-  return in_conflict_64<D>(v, key, q, qkey, t, err);
+  return in_conflict_64<D, XT>(v, key, q, qkey, t, err);
 }
 
 // exit_face on split coordinates (same contract as exit_face).

@@ -291,6 +291,10 @@ class DelaunayTree:
         _check(_native.load().vd_set_early_phase(self._h, int(until_inserted), int(thin), float(ratio)),
                "set_early_phase")
 
+    def set_exact_tier(self, mode=0, switch_after=32):
+        """Exact tier of the conflict tests: 0 automatic, 1 expansions only, 2 integer first (see vd_set_exact_tier)."""
+        _check(_native.load().vd_set_exact_tier(self._h, int(mode), int(switch_after)), "set_exact_tier")
+
     def set_small_rounds(self, max_active=16384):
         """Run rounds in one cooperative launch while fewer points are active (0: never)."""
         _check(_native.load().vd_set_small_rounds(self._h, int(max_active)), "set_small_rounds")
