@@ -53,6 +53,15 @@ struct Cap;
 #ifndef VD_CAVITY_MIN_BLOCKS
 #define VD_CAVITY_MIN_BLOCKS 5
 #endif
+// resident 256-thread blocks per SM asked of the point-walk kernels (0: no bound)
+#ifndef VD_WALK_MIN_BLOCKS
+#define VD_WALK_MIN_BLOCKS 2
+#endif
+#if VD_WALK_MIN_BLOCKS > 0
+#define VD_WALK_BOUNDS __launch_bounds__(256, VD_WALK_MIN_BLOCKS)
+#else
+#define VD_WALK_BOUNDS
+#endif
 template <>
 struct Cap<3> {
   static constexpr int MAXC = VD_CAP3_C, MAXF = VD_CAP3_F, HS = VD_CAP3_H;
@@ -402,7 +411,7 @@ __device__ __forceinline__ void activate_body(DevTree T, unsigned long long seed
   flush_tally(T.ctr, tl, 0, walk);
 }
 template <int D>
-__global__ void k_activate(DevTree T, unsigned long long seed) { activate_body<D>(T, seed, blockIdx.x, gridDim.x); }
+__global__ void VD_WALK_BOUNDS k_activate(DevTree T, unsigned long long seed) { activate_body<D>(T, seed, blockIdx.x, gridDim.x); }
 
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void pick_body(DevTree T, int thin, int bid, int nblk) {
@@ -444,6 +453,29 @@ __device__ __forceinline__ void pick_body(DevTree T, int thin, int bid, int nblk
   if ((threadIdx.x & 31) == 0 && ncand) atomicAdd(&T.ctr->candidates, ncand);
 }
 __global__ void k_pick(DevTree T, int thin) { pick_body(T, thin, blockIdx.x, gridDim.x); }
+
+// Headers of a warp's items in a grid-stride loop over a candidate list,
+// staged in shared memory: lane k loads item it0 + k * nw (its candidate,
+// candidate record and state), one round trip for up to 32 items instead of
+// three dependent loads per item.
+struct HeadBuf {
+  int c[32];
+  int4 cd[32];
+  int4 info[32];
+};
+__device__ __forceinline__ int load_heads(const DevTree& T, HeadBuf& H, const int* list, int it0, int nin, int nw,
+                                          int lane) {
+  const int n = min(32, (nin - it0 + nw - 1) / nw);
+  __syncwarp();  // the previous batch is read
+  if (lane < n) {
+    const int c = list[it0 + lane * nw];
+    H.c[lane] = c;
+    H.cd[lane] = T.cand[c];
+    H.info[lane] = T.cinfo[c];
+  }
+  __syncwarp();
+  return n;
+}
 
 // Storage of one cavity search: shared memory for the common case, a
 // reserved, 16-byte aligned stretch of the round's cavity pool when that
@@ -808,6 +840,7 @@ struct WarpCommit {
   int id[Cap<D>::MAXF];
   int first[Cap<D>::MAXC];     // first facet index of each cavity simplex
   int freeslot[Cap<D>::MAXC];  // cavity slots without an own facet
+  HeadBuf hb;
 };
 
 
@@ -896,19 +929,14 @@ __device__ void write_star(const DevTree& T, WarpCommit<D>& W, const int* __rest
           break;
         }
       }
+      // the partner half-ridge (m, g') lies on face g' of new simplex m: the
+      // face opposite its vertex outside the ridge
       const int m = other >> 2;
-      int pos = -1;
-      if (other >= 0 && m < nfac) {
-        const int* w = FR + 6 * m;
-        const int qm = w[5] & 3;
-        for (int i = 0; i < NV; ++i)
-          if (i != qm && w[i] != r0 && w[i] != r1) pos = i;
-      }
-      if (pos < 0) {
+      if (other < 0 || m >= nfac) {
         set_error(T.ctr, E_INTERNAL);
         continue;
       }
-      nn = set4(nn, g, (W.id[m] << 2) | pos);
+      nn = set4(nn, g, (W.id[m] << 2) | (other & 3));
     }
     emit_simplex(T, r, W.id[j], nn, round);
   }
@@ -970,17 +998,11 @@ __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, i
         continue;
       }
       const int m = other >> 2;
-      const int* w = FR + 6 * m;
-      // face of m opposite its vertex outside the ridge (and not the new vertex)
-      const int qm = w[5] & 3;
-      int pos = -1;
-      for (int i = 0; i < NV; ++i)
-        if (i != qm && w[i] != r0 && w[i] != r1) pos = i;
-      if (pos < 0) {
+      if (m >= nfac) {
         set_error(T.ctr, E_INTERNAL);
         continue;
       }
-      nn = set4(nn, g, (ID[m] << 2) | pos);
+      nn = set4(nn, g, (ID[m] << 2) | (other & 3));
     }
     emit_simplex(T, r, ID[j], nn, round);
   }
@@ -1017,7 +1039,9 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
   const int sin = 2 * pass, sout = 2 * pass + 1;
   constexpr int MAXF = Cap<D>::MAXF, MAXC = Cap<D>::MAXC;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // MODE 1 gets only the item headers in shared memory, the others a WarpCommit each
   WarpCommit<D>& W = reinterpret_cast<WarpCommit<D>*>(dsm)[wib];
+  HeadBuf& H = MODE == 1 ? reinterpret_cast<HeadBuf*>(dsm)[wib] : W.hb;
   const unsigned long long pe = pass_epoch(round, pass);
   const int par = round & 1;
   unsigned long long nwon = 0, ncreated = 0, nkilled = 0;
@@ -1030,181 +1054,187 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
   const int nw = nblk * 4;
   const int lo = MODE == 2 ? T.ctr->win_lo : 0;
   const int nin = MODE == 2 ? T.ctr->nwin : T.ctr->nwl[sin];
-  for (int it = lo + bid * 4 + wib; it < nin; it += nw) {
-    const int c = MODE == 2 ? T.win[it] : T.wl[sin & 1][it];
-    const int4 info = T.cinfo[c];
-    if (info.w != (MODE == 2 ? ST_WIN : ST_OK)) continue;
-    const int4 cd = T.cand[c];
-    const unsigned long long key = pe | (unsigned)cd.z;
-    int *P, *F, ncav, nfac;
-    bool big;
-    cand_lists(T, info, P, F, ncav, nfac, big);
-    int base;
-    if (MODE != 2) {
-      bool ok = true;
-      for (int i = lane; i < ncav; i += 32) {
-        const int s = P[i];
-        if (bad_simp(T, s)) {
-          ok = false;
-          continue;
-        }
-        ok = ok && T.claim_c[s] == key && (MODE == 1 || T.claim_n[s] > key);
-      }
-      for (int j = lane; j < nfac && ok; j += 32) {
-        const int o = F[6 * j + 4];
-        if (o < 0) continue;
-        if (bad_simp(T, o >> 2)) {
-          ok = false;
-          continue;
-        }
-        const unsigned long long ko = T.claim_c[o >> 2];
-        if (MODE == 0) {
-          ok = ko > key;
-        } else if (ko < key) {
-          // the lower candidate X whose cavity holds the outer simplex
-          const int xv = (int)vertex_of_priority((uint32_t)ko, seed);
-          if (bad_vert(T, xv)) {
+  const int* list = MODE == 2 ? T.win : T.wl[sin & 1];
+  for (int it0 = lo + bid * 4 + wib; it0 < nin; it0 += 32 * nw) {
+    // lane k loads the list entry, state and candidate record of the warp's
+    // k-th next item: one round trip for up to 32 items instead of three each
+    const int nh = load_heads(T, H, list, it0, nin, nw, lane);
+    for (int k = 0; k < nh; ++k) {
+      const int c = H.c[k];
+      const int4 info = H.info[k];
+      if (info.w != (MODE == 2 ? ST_WIN : ST_OK)) continue;
+      const int4 cd = H.cd[k];
+      const unsigned long long key = pe | (unsigned)cd.z;
+      int *P, *F, ncav, nfac;
+      bool big;
+      cand_lists(T, info, P, F, ncav, nfac, big);
+      int base;
+      if (MODE != 2) {
+        bool ok = true;
+        for (int i = lane; i < ncav; i += 32) {
+          const int s = P[i];
+          if (bad_simp(T, s)) {
             ok = false;
             continue;
           }
-          const int* r = F + 6 * j;
-          vdp::FPt fv[NV];
-          for (int i = 0; i < NV; ++i) fv[i] = load_fpt(T, r[i]);
-          const vdp::FPt fx = load_fpt(T, xv);
-          auto load64 = [&](vdp::VPt* v64, vdp::VPt& p64) {
-            for (int i = 0; i < NV; ++i) v64[i] = load_pt(T, r[i]);
-            p64 = load_pt(T, xv);
-          };
-          ok = !vdp::in_conflict_hl<D, XT>(fv, r, fx, xv, tl, perr, load64);
+          ok = ok && T.claim_c[s] == key && (MODE == 1 || T.claim_n[s] > key);
         }
-      }
-      if (!__all_sync(FULL, ok)) {
-        if (lane == 0) {
-          if (last) {
-            T.cinfo[c].w = ST_LOST;
-          } else {
-            const int k = atomicAdd(&T.ctr->nwl[sout], 1);
-            T.wl[sout & 1][k] = c;
+        for (int j = lane; j < nfac && ok; j += 32) {
+          const int o = F[6 * j + 4];
+          if (o < 0) continue;
+          if (bad_simp(T, o >> 2)) {
+            ok = false;
+            continue;
+          }
+          const unsigned long long ko = T.claim_c[o >> 2];
+          if (MODE == 0) {
+            ok = ko > key;
+          } else if (ko < key) {
+            // the lower candidate X whose cavity holds the outer simplex
+            const int xv = (int)vertex_of_priority((uint32_t)ko, seed);
+            if (bad_vert(T, xv)) {
+              ok = false;
+              continue;
+            }
+            const int* r = F + 6 * j;
+            vdp::FPt fv[NV];
+            for (int i = 0; i < NV; ++i) fv[i] = load_fpt(T, r[i]);
+            const vdp::FPt fx = load_fpt(T, xv);
+            auto load64 = [&](vdp::VPt* v64, vdp::VPt& p64) {
+              for (int i = 0; i < NV; ++i) v64[i] = load_pt(T, r[i]);
+              p64 = load_pt(T, xv);
+            };
+            ok = !vdp::in_conflict_hl<D, XT>(fv, r, fx, xv, tl, perr, load64);
           }
         }
-        continue;
-      }
-      const int fresh = max(0, nfac - ncav);
-      if (fresh > chunk.y) {
-        const int take = max(fresh, kSlotChunk);
-        int b0 = 0;
-        if (lane == 0) b0 = atomicAdd(&T.ctr->nsimp, take);
-        b0 = __shfl_sync(FULL, b0, 0);
-        chunk = make_int2(b0, take);
-        if (b0 + take > T.cap_simp) {
+        if (!__all_sync(FULL, ok)) {
           if (lane == 0) {
-            atomicAdd(&T.ctr->wasted, take);
-            atomicExch(&T.ctr->simp_overflow, 1);
+            if (last) {
+              T.cinfo[c].w = ST_LOST;
+            } else {
+              const int k = atomicAdd(&T.ctr->nwl[sout], 1);
+              T.wl[sout & 1][k] = c;
+            }
           }
-          chunk = make_int2(0, 0);
+          continue;
         }
+        const int fresh = max(0, nfac - ncav);
+        if (fresh > chunk.y) {
+          const int take = max(fresh, kSlotChunk);
+          int b0 = 0;
+          if (lane == 0) b0 = atomicAdd(&T.ctr->nsimp, take);
+          b0 = __shfl_sync(FULL, b0, 0);
+          chunk = make_int2(b0, take);
+          if (b0 + take > T.cap_simp) {
+            if (lane == 0) {
+              atomicAdd(&T.ctr->wasted, take);
+              atomicExch(&T.ctr->simp_overflow, 1);
+            }
+            chunk = make_int2(0, 0);
+          }
+        }
+        if (fresh > chunk.y) {
+          if (lane == 0) T.cinfo[c].w = ST_LOST;
+          continue;
+        }
+        base = chunk.x;
+        chunk.x += fresh;
+        chunk.y -= fresh;
+        for (int i = lane; i < ncav; i += 32) T.killed[P[i]] = make_int2(round, cd.x);
+        ++nwon;
+        if (MODE == 1) {
+          if (lane == 0) {
+            T.cand[c].y = base;  // the home simplex is not needed any more
+            T.cinfo[c].w = ST_WIN;
+            T.win[atomicAdd(&T.ctr->nwin, 1)] = c;
+          }
+          __syncwarp();
+          continue;
+        }
+      } else {
+        base = cd.y;
       }
-      if (fresh > chunk.y) {
-        if (lane == 0) T.cinfo[c].w = ST_LOST;
-        continue;
-      }
-      base = chunk.x;
-      chunk.x += fresh;
-      chunk.y -= fresh;
-      for (int i = lane; i < ncav; i += 32) T.killed[P[i]] = make_int2(round, cd.x);
-      ++nwon;
-      if (MODE == 1) {
-        if (lane == 0) {
-          T.cand[c].y = base;  // the home simplex is not needed any more
-          T.cinfo[c].w = ST_WIN;
-          T.win[atomicAdd(&T.ctr->nwin, 1)] = c;
+      int id0;
+      const int* IDS;
+      if (!big && nfac <= MAXF && ncav <= MAXC) {
+        // slot assignment: first facet of cavity simplex k takes k's slot;
+        // the other facets take the remaining cavity slots, then fresh ones
+        for (int i = lane; i < ncav; i += 32) W.first[i] = 0x7fffffff;
+        __syncwarp();
+        for (int j = lane; j < nfac; j += 32) atomicMin(&W.first[__ldg(F + 6 * j + 5) >> 2], j);
+        __syncwarp();
+        int nfree = 0;  // cavity slots without an own facet, ranked
+        for (int i0 = 0; i0 < ncav; i0 += 32) {
+          const int i = i0 + lane;
+          const bool fr = i < ncav && W.first[i] == 0x7fffffff;
+          const unsigned m = __ballot_sync(FULL, fr);
+          if (fr) W.freeslot[nfree + __popc(m & ((1u << lane) - 1))] = P[i];
+          nfree += __popc(m);
+        }
+        int nsec = 0;  // facets that are not the first of their cavity simplex
+        for (int j0 = 0; j0 < nfac; j0 += 32) {
+          const int j = j0 + lane;
+          int id = 0;
+          bool sec = false;
+          if (j < nfac) {
+            const int k = __ldg(F + 6 * j + 5) >> 2;
+            sec = W.first[k] != j;
+            if (!sec) id = P[k];
+          }
+          const unsigned m = __ballot_sync(FULL, sec);
+          if (sec) {
+            const int t = nsec + __popc(m & ((1u << lane) - 1));
+            id = t < nfree ? W.freeslot[t] : base + (t - nfree);
+          }
+          if (j < nfac) W.id[j] = id;
+          nsec += __popc(m);
         }
         __syncwarp();
-        continue;
+        id0 = W.id[0];
+        IDS = W.id;
+        // leftover cavity slots become holes pointing into the star
+        for (int t = nsec + lane; t < nfree; t += 32)
+          store_simplex(T, W.freeslot[t], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
+        write_star<D>(T, W, F, nfac, cd.x, round, lane);
+      } else {
+        // large star (spilled search): plain slot assignment, ids in the
+        // stretch's vertex-list area (free after the search), ridge table in
+        // its own area
+        int* ID = P + kOffCV;
+        for (int j = lane; j < nfac; j += 32) ID[j] = j < ncav ? P[j] : base + (j - ncav);
+        __syncwarp();
+        id0 = ID[0];
+        IDS = ID;
+        for (int i = nfac + lane; i < ncav; i += 32)
+          store_simplex(T, P[i], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
+        write_star_big<D>(T, F, ID, nfac, round, P + kOffR, lane);
       }
-    } else {
-      base = cd.y;
-    }
-    int id0;
-    const int* IDS;
-    if (!big && nfac <= MAXF && ncav <= MAXC) {
-      // slot assignment: first facet of cavity simplex k takes k's slot;
-      // the other facets take the remaining cavity slots, then fresh ones
-      for (int i = lane; i < ncav; i += 32) W.first[i] = 0x7fffffff;
-      __syncwarp();
-      for (int j = lane; j < nfac; j += 32) atomicMin(&W.first[__ldg(F + 6 * j + 5) >> 2], j);
-      __syncwarp();
-      int nfree = 0;  // cavity slots without an own facet, ranked
-      for (int i0 = 0; i0 < ncav; i0 += 32) {
-        const int i = i0 + lane;
-        const bool fr = i < ncav && W.first[i] == 0x7fffffff;
-        const unsigned m = __ballot_sync(FULL, fr);
-        if (fr) W.freeslot[nfree + __popc(m & ((1u << lane) - 1))] = P[i];
-        nfree += __popc(m);
-      }
-      int nsec = 0;  // facets that are not the first of their cavity simplex
-      for (int j0 = 0; j0 < nfac; j0 += 32) {
-        const int j = j0 + lane;
-        int id = 0;
-        bool sec = false;
-        if (j < nfac) {
-          const int k = __ldg(F + 6 * j + 5) >> 2;
-          sec = W.first[k] != j;
-          if (!sec) id = P[k];
+      if (MODE == 2) {
+        // facets shared with another winner's cavity: publish this side's new
+        // simplex and remember where the other side's goes (fix_body)
+        __syncwarp();
+        for (int j = lane; j < nfac; j += 32) {
+          const int o = F[6 * j + 4];
+          if (o < 0 || bad_simp(T, o >> 2) || T.killed[o >> 2].x != round) continue;
+          const int kf = F[6 * j + 5], qf = kf & 3, k = kf >> 2;
+          const int inner = (P[k] << 2) | (kf & 3);  // the removed simplex and its face on this facet
+          (void)qf;
+          T.repl[inner] = (IDS[j] << 2) | (kf & 3);
+          F[6 * j] = IDS[j];
+          F[6 * j + 1] = kf & 3;
+          F[6 * j + 2] = -2;
         }
-        const unsigned m = __ballot_sync(FULL, sec);
-        if (sec) {
-          const int t = nsec + __popc(m & ((1u << lane) - 1));
-          id = t < nfree ? W.freeslot[t] : base + (t - nfree);
-        }
-        if (j < nfac) W.id[j] = id;
-        nsec += __popc(m);
       }
-      __syncwarp();
-      id0 = W.id[0];
-      IDS = W.id;
-      // leftover cavity slots become holes pointing into the star
-      for (int t = nsec + lane; t < nfree; t += 32)
-        store_simplex(T, W.freeslot[t], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
-      write_star<D>(T, W, F, nfac, cd.x, round, lane);
-    } else {
-      // large star (spilled search): plain slot assignment, ids in the
-      // stretch's vertex-list area (free after the search), ridge table in
-      // its own area
-      int* ID = P + kOffCV;
-      for (int j = lane; j < nfac; j += 32) ID[j] = j < ncav ? P[j] : base + (j - ncav);
-      __syncwarp();
-      id0 = ID[0];
-      IDS = ID;
-      for (int i = nfac + lane; i < ncav; i += 32)
-        store_simplex(T, P[i], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
-      write_star_big<D>(T, F, ID, nfac, round, P + kOffR, lane);
-    }
-    if (MODE == 2) {
-      // facets shared with another winner's cavity: publish this side's new
-      // simplex and remember where the other side's goes (fix_body)
-      __syncwarp();
-      for (int j = lane; j < nfac; j += 32) {
-        const int o = F[6 * j + 4];
-        if (o < 0 || bad_simp(T, o >> 2) || T.killed[o >> 2].x != round) continue;
-        const int kf = F[6 * j + 5], qf = kf & 3, k = kf >> 2;
-        const int inner = (P[k] << 2) | (kf & 3);  // the removed simplex and its face on this facet
-        (void)qf;
-        T.repl[inner] = (IDS[j] << 2) | (kf & 3);
-        F[6 * j] = IDS[j];
-        F[6 * j + 1] = kf & 3;
-        F[6 * j + 2] = -2;
+      if (lane == 0) {
+        write_hints<D>(T, cd.x, load_pt(T, cd.x), id0);
+        T.cinfo[c].w = ST_DONE;
+        T.act[par][cd.w].x = -1;
       }
+      ncreated += nfac;
+      nkilled += ncav;
+      nholes += max(0, ncav - nfac);
+      __syncwarp();
     }
-    if (lane == 0) {
-      write_hints<D>(T, cd.x, load_pt(T, cd.x), id0);
-      T.cinfo[c].w = ST_DONE;
-      T.act[par][cd.w].x = -1;
-    }
-    ncreated += nfac;
-    nkilled += ncav;
-    nholes += max(0, ncav - nfac);
-    __syncwarp();
   }
   if (perr) set_error(T.ctr, E_PRECISION);
   if (MODE == 1) flush_tally(T.ctr, tl, 0, 0);
@@ -1378,7 +1408,7 @@ __device__ __forceinline__ void relocate_body(DevTree T, int bid, int nblk) {
   flush_tally(T.ctr, tl, 0, walk);
 }
 template <int D>
-__global__ void k_relocate(DevTree T) { relocate_body<D>(T, blockIdx.x, gridDim.x); }
+__global__ void VD_WALK_BOUNDS k_relocate(DevTree T) { relocate_body<D>(T, blockIdx.x, gridDim.x); }
 
 // ---------------------------------------------------------------------------
 // Small rounds in one launch.  While few points are active a round is a
@@ -1503,9 +1533,9 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
     }
     if (tu.adjacent) {
       if (tu.exact_int)
-        k_check<D, 1, 1><<<L.warps / 4, 128, 0, L.stream>>>(T, p, last, fd.seed);
+        k_check<D, 1, 1><<<L.warps / 4, 128, 4 * sizeof(HeadBuf), L.stream>>>(T, p, last, fd.seed);
       else
-        k_check<D, 1, 0><<<L.warps / 4, 128, 0, L.stream>>>(T, p, last, fd.seed);
+        k_check<D, 1, 0><<<L.warps / 4, 128, 4 * sizeof(HeadBuf), L.stream>>>(T, p, last, fd.seed);
       mark(KT_DECIDE);
       k_check<D, 2, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
     } else if (tu.exact_int) {
