@@ -283,7 +283,7 @@ vd_tree* vd_tree_create(int dim, void* stream, int* status);
  * them as batched builds, so that requests arriving while others run are
  * admitted as slots and budget free up, and batches of different slots
  * overlap on the device.  Admission: the estimated device bytes of the
- * requests in flight (3D 360 B/point, 2D 100 B/point, 1.5x slack included)
+ * requests in flight (3D 1850 B/point, 2D 700 B/point, 1.5x slack included)
  * stay within `pool_bytes`; a request larger than the budget finishes with
  * VD_ERR_NOMEM.  `max_batch_points` caps a batch (0 = only the budget).
  * Each result is the triangulation of the request alone. */

@@ -53,7 +53,7 @@ def test_mixed_stream_same_as_alone(vd):
 
 def test_admission_respects_budget(vd):
     reqs = W.c5_requests(24, lo=1000, hi=5000, seed=777)
-    budget = 3 * 360 * 5000  # room for about three of the largest 3D requests
+    budget = 3 * 1850 * 5000  # room for about three of the largest 3D requests
     srv = vd.Server(pool_bytes=budget, slots=4)
     ids = [srv.submit(W.c5_points(r)) for r in reqs]
     drain(srv, ids)

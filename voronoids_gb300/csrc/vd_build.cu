@@ -832,17 +832,17 @@ __device__ __forceinline__ void cand_lists(const DevTree& T, const int4& info, i
 
 template <int D>
 struct WarpCommit {
-  // ridge table slots: a star of f facets has f D / 2 ridges, at most 288
-  // (3D, 192 facets) or 96 (2D, 96 facets): load factor <= 0.56 / 0.375
-  static constexpr int HR = D == 3 ? 512 : 256;
+  // ridge table: a star of f facets has f D / 2 ridges; the table is paired
+  // in sweeps of at most 2/3 HR ridges each (one sweep below 170 ridges in
+  // 3D, 85 in 2D)
+  static constexpr int HR = D == 3 ? 256 : 128;
   unsigned long long rk[HR];   // ridge key (r0 << 32 | r1)
-  int ra[HR], rb[HR];          // the two half-ridges (facet << 2 | face)
+  int ra[HR];                  // first half-ridge to arrive (facet << 2 | face), -2 once paired
   int id[Cap<D>::MAXF];
   int first[Cap<D>::MAXC];     // first facet index of each cavity simplex
   int freeslot[Cap<D>::MAXC];  // cavity slots without an own facet
   HeadBuf hb;
 };
-
 
 // Ridge of face g of new simplex r (vertices r[0..3], new vertex at qf): the
 // vertices other than r[g] and the new vertex, smaller first (2D: one vertex).
@@ -876,69 +876,68 @@ __device__ __forceinline__ void emit_simplex(const DevTree& T, const int* r, int
   }
 }
 
-// Star of one winner, small case: the half-ridges of all new simplices go
-// into a shared-memory table keyed by the ridge's vertices; each ridge has
-// exactly two halves, which are each other's neighbours.
+// Star of one winner, small case.  The new simplices are written first, each
+// with its outer neighbour; then their faces through the new vertex are
+// paired.  Such a face is determined by its ridge (its vertices other than
+// the new vertex), and every ridge of the star belongs to exactly two new
+// simplices.  The half-ridges go into a shared-memory table keyed by the
+// ridge; the second half of a ridge to arrive finds the first and writes the
+// two links.  A star with more ridges than 2/3 of the table is paired in
+// several sweeps, each over the ridges of one residue of the key hash.
+__device__ __forceinline__ unsigned ridge_hash(int r0, int r1) {
+  return ((unsigned)r0 * 0x9E3779B1u) ^ ((unsigned)r1 * 0x85EBCA77u);
+}
 template <int D>
 __device__ void write_star(const DevTree& T, WarpCommit<D>& W, const int* __restrict__ FR, int nfac, int qv,
                            int round, int lane) {
   constexpr int NV = D + 1;
-  // table size: a power of two at least twice the ridges, within WarpCommit::HR
   constexpr int HR = WarpCommit<D>::HR;
+  constexpr int LOG_HR = D == 3 ? 8 : 7;
+  constexpr int PER_SWEEP = 2 * HR / 3;
   const unsigned long long EMPTY = ~0ull;
-  for (int i = lane; i < HR; i += 32) {
-    W.rk[i] = EMPTY;
-    W.ra[i] = -1;
-  }
-  __syncwarp();
-  for (int it = lane; it < nfac * NV; it += 32) {
-    const int j = it / NV, g = it - j * NV;
-    const int* r = FR + 6 * j;
-    const int qf = r[5] & 3;
-    if (g == qf) continue;
-    int r0, r1;
-    ridge_of<D>(r, g, qf, r0, r1);
-    const unsigned long long key = ((unsigned long long)(unsigned)r0 << 32) | (unsigned)r1;
-    unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> 40) & (HR - 1);
-    for (int probe = 0; probe < HR; ++probe, h = (h + 1) & (HR - 1)) {
-      const unsigned long long old = atomicCAS(&W.rk[h], EMPTY, key);
-      if (old == EMPTY || old == key) {
-        if (atomicCAS(&W.ra[h], -1, (j << 2) | g) != -1) W.rb[h] = (j << 2) | g;
-        break;
-      }
-    }
-  }
-  __syncwarp();
   for (int j = lane; j < nfac; j += 32) {
     const int* r = FR + 6 * j;
     const int qf = r[5] & 3;
-    int4 nn = make_int4(-1, -1, -1, -1);
-    nn = set4(nn, qf, r[4]);
-    for (int g = 0; g < NV; ++g) {
+    emit_simplex(T, r, W.id[j], set4(make_int4(-1, -1, -1, -1), qf, r[4]), round);
+  }
+  const int sweeps = (nfac * D / 2 + PER_SWEEP - 1) / PER_SWEEP;
+  for (int sw = 0; sw < sweeps; ++sw) {
+    for (int i = lane; i < HR; i += 32) {
+      W.rk[i] = EMPTY;
+      W.ra[i] = -1;
+    }
+    __syncwarp();  // also orders the record stores above before the link stores below
+    for (int it = lane; it < nfac * NV; it += 32) {
+      const int j = it / NV, g = it - j * NV;
+      const int* r = FR + 6 * j;
+      const int qf = r[5] & 3;
       if (g == qf) continue;
       int r0, r1;
       ridge_of<D>(r, g, qf, r0, r1);
+      const unsigned hv = ridge_hash(r0, r1);
+      if (sweeps > 1 && (int)((hv & 0xffffu) % (unsigned)sweeps) != sw) continue;
       const unsigned long long key = ((unsigned long long)(unsigned)r0 << 32) | (unsigned)r1;
-      unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> 40) & (HR - 1);
-      int other = -1;
+      const int mine = (j << 2) | g;
+      unsigned h = hv >> (32 - LOG_HR);
       for (int probe = 0; probe < HR; ++probe, h = (h + 1) & (HR - 1)) {
-        const unsigned long long k2 = W.rk[h];
-        if (k2 == EMPTY) break;
-        if (k2 == key) {
-          other = W.ra[h] == ((j << 2) | g) ? W.rb[h] : W.ra[h];
-          break;
+        const unsigned long long old = atomicCAS(&W.rk[h], EMPTY, key);
+        if (old != EMPTY && old != key) continue;
+        const int other = atomicCAS(&W.ra[h], -1, mine);
+        if (other >= 0) {
+          // second half: link both new simplices across the ridge
+          W.ra[h] = -2;
+          const int m = other >> 2, gm = other & 3;
+          reinterpret_cast<int*>(T.simp + W.id[j])[4 + g] = (W.id[m] << 2) | gm;
+          reinterpret_cast<int*>(T.simp + W.id[m])[4 + gm] = (W.id[j] << 2) | g;
         }
+        break;
       }
-      // the partner half-ridge (m, g') lies on face g' of new simplex m: the
-      // face opposite its vertex outside the ridge
-      const int m = other >> 2;
-      if (other < 0 || m >= nfac) {
-        set_error(T.ctr, E_INTERNAL);
-        continue;
-      }
-      nn = set4(nn, g, (W.id[m] << 2) | (other & 3));
     }
-    emit_simplex(T, r, W.id[j], nn, round);
+    __syncwarp();
+    // a ridge with one half would be a broken star
+    for (int i = lane; i < HR; i += 32)
+      if (W.ra[i] >= 0) set_error(T.ctr, E_INTERNAL);
+    __syncwarp();
   }
 }
 
@@ -1495,8 +1494,10 @@ constexpr size_t small_rounds_smem() {
   return 4 * sizeof(WarpCav<D>) > 4 * sizeof(WarpCommit<D>) ? 4 * sizeof(WarpCav<D>) : 4 * sizeof(WarpCommit<D>);
 }
 
-// Resident blocks of k_check<2>, k_check<3> on the whole GPU.
+// Resident blocks on the whole GPU of the strict-mode k_check (MODE 0) and
+// of the commit half (MODE 2), 2D and 3D.
 int g_check_wave[2] = {1 << 20, 1 << 20};
+int g_commit_wave[2] = {1 << 20, 1 << 20};
 // Grid of the small-round kernel (0: not available).
 int g_small_grid[2] = {0, 0};
 
@@ -1524,7 +1525,10 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
   else
     k_cavity<D, 0><<<L.warps / 4, 128, 0, L.stream>>>(T, tu.adjacent);
   mark(KT_CAVITY);
-  const int commit_grid = std::min(L.warps / 4, g_check_wave[D - 2]);
+  // the commit half needs little shared memory per warp and few registers,
+  // so it runs up to twice the warps of the search (one resident wave)
+  const int commit_grid = std::min(L.warps / 2, g_commit_wave[D - 2]);
+  const int strict_grid = std::min(L.warps / 4, g_check_wave[D - 2]);
   for (int p = 0; p < tu.passes; ++p) {
     const int last = p == tu.passes - 1;
     if (p > 0) {
@@ -1539,9 +1543,9 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
       mark(KT_DECIDE);
       k_check<D, 2, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
     } else if (tu.exact_int) {
-      k_check<D, 0, 1><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
+      k_check<D, 0, 1><<<strict_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
     } else {
-      k_check<D, 0, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
+      k_check<D, 0, 0><<<strict_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
     }
     mark(KT_CHECK);
   }
@@ -1587,14 +1591,18 @@ int prepare_once() {
   attr((const void*)k_check<2, 2, 0>, 4 * (int)sizeof(WarpCommit<2>));
   if (e != cudaSuccess) return E_CUDA;
   // k_check is a grid-stride loop: one resident wave avoids a ragged second
-  int dev = 0, sms = 0, b3 = 0, b2 = 0;
+  int dev = 0, sms = 0, b3 = 0, b2 = 0, c3 = 0, c2 = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_check<3, 0, 1>, 128, 4 * sizeof(WarpCommit<3>)) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_check<2, 0, 1>, 128, 4 * sizeof(WarpCommit<2>)) != cudaSuccess)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_check<2, 0, 1>, 128, 4 * sizeof(WarpCommit<2>)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c3, k_check<3, 2, 0>, 128, 4 * sizeof(WarpCommit<3>)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, k_check<2, 2, 0>, 128, 4 * sizeof(WarpCommit<2>)) != cudaSuccess)
     return E_CUDA;
   g_check_wave[1] = std::max(1, sms * b3);
   g_check_wave[0] = std::max(1, sms * b2);
+  g_commit_wave[1] = std::max(1, sms * c3);
+  g_commit_wave[0] = std::max(1, sms * c2);
   // small-round kernel: one block per SM when a block fits
   int s3 = 0, s2 = 0;
   cudaFuncSetAttribute((const void*)k_rounds_small<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -212,6 +212,8 @@ struct vd_tree {
 namespace {
 
 constexpr int kMaxWarpsPerSm = 32;
+// per-warp fresh-slot chunks: room for the widest k_check grid per SM
+constexpr int kChunkWarpsPerSm = 64;
 
 vd::Launch launch_of(const vd_tree* t) {
   vd::Launch L;
@@ -487,7 +489,7 @@ int alloc_tree(vd_tree* t, int dim, void* stream) {
       dalloc(&t->T.lev_off, vd::kMaxLevels + 1))
     return vd::E_NOMEM;
   if (cudaMallocHost((void**)&t->h_mm, 8 * sizeof(unsigned long long)) != cudaSuccess) return vd::E_NOMEM;
-  t->T.cap_wchunk = t->sms * kMaxWarpsPerSm;
+  t->T.cap_wchunk = t->sms * kChunkWarpsPerSm;
   if (dalloc(&t->T.wchunk, t->T.cap_wchunk)) return vd::E_NOMEM;
   t->ncells = vd::hint_cells(dim, single_hint_levels(dim));
   if (dalloc(&t->T.hint, t->ncells)) return vd::E_NOMEM;

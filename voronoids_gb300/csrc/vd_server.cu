@@ -28,9 +28,11 @@
 
 namespace {
 
-// Estimated device bytes of a request: simplex arrays, point records and the
-// cavity pool of its build, with 1.5x slack.
-int64_t estimate_bytes(int dim, int64_t n) { return (dim == 3 ? 360 : 100) * std::max<int64_t>(n, 1) + 4096; }
+// Estimated device bytes of a request, with 1.5x slack: simplex slots (3D
+// 7.6, 2D 2.3 per point, 92 B each: record, claims, marks, star links) and
+// per-point records, work lists and edge scratch (about 520 B in 3D, 250 B
+// in 2D).
+int64_t estimate_bytes(int dim, int64_t n) { return (dim == 3 ? 1850 : 700) * std::max<int64_t>(n, 1) + 4096; }
 
 struct Request {
   int64_t id;
