@@ -70,7 +70,8 @@ typedef struct vd_stats {
   int64_t searched;          /* nominations that won the thinning claim and were searched */
   int64_t won_pass[3];       /* insertions decided in resolution pass 0, 1, 2 and later */
   int64_t spilled;           /* cavity searches that spilled to the pool */
-  int64_t max_search_levels; /* deepest conflict-region search (breadth-first levels) */
+  int64_t max_search_levels; /* longest conflict-region search in waves of 32 (simplex, face)
+                                tests, when above 64 (0 otherwise) */
 } vd_stats;
 
 /* DelaunayTree::<3,4>::new / ::<2,3>::new

@@ -547,21 +547,23 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
   __syncwarp();
   if (lane == 0) hset_insert(S.hk, S.hs, start);
   __syncwarp();
+  // (simplex, face) items are taken in waves of 32 in discovery order, not
+  // level by level: a wave also takes the items of simplices the previous
+  // wave appended, so a search needs about items / 32 dependent rounds of
+  // gathers rather than one or more per level
   int head = 0, levels = 0;
   while (true) {
-    const int hi = min(*(volatile int*)&ctl.ncav, S.maxc);
-    if (*(volatile int*)&ctl.flags || head >= hi) break;
+    const int avail = min(*(volatile int*)&ctl.ncav, S.maxc) * NV;
+    if (*(volatile int*)&ctl.flags || head >= avail) break;
     ++levels;
-    const int items = (hi - head) * NV;
-    for (int it = lane; it < items; it += 32) {
-      const int k = head + it / NV, f = it - (it / NV) * NV;
+    const int it = head + lane;
+    if (it < avail) {
+      const int k = it / NV, f = it - k * NV;
       const int code = get4(S.cn[k], f);
       bool facet = code < 0;
-      if (!facet && bad_simp(T, code >> 2)) {
-        set_error(T.ctr, E_INTERNAL);
-        continue;
-      }
-      if (!facet) {
+      const bool broken = !facet && bad_simp(T, code >> 2);
+      if (broken) set_error(T.ctr, E_INTERNAL);
+      if (!facet && !broken) {
         const int nb = code >> 2;
         if (!hset_find(S.hk, S.hs, nb)) {
           int4 vv, nn;
@@ -610,7 +612,7 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
       }
     }
     __syncwarp();
-    head = hi;
+    head += min(32, avail - head);
   }
   __syncwarp();
   if (lane == 0 && levels > 64) atomicMax(&T.ctr->max_levels, levels);
