@@ -199,17 +199,26 @@ __global__ void k_upload(DevTree T, const double* xyz, long long n, int base) {
 // cell keeps the slot of a simplex created near it (written by every winner,
 // races are harmless: any live simplex of the set is a valid walk start, a
 // near one is a short walk).
+//
+// Cell of p at the finest level of set g, per axis.  The coordinate map is
+// the only FP64 work (the FP64 pipe of this GPU is narrow); the cell of a
+// coarser level l is this one shifted right by hint_levels - l, the same
+// cell as floor(u * 2^l) gives directly.
 template <int D>
-__device__ __forceinline__ int hint_index(const SetGeo& g, const vdp::VPt& p, int level) {
-  const int side = 1 << level;
+__device__ __forceinline__ void hint_cell(const SetGeo& g, const vdp::VPt& p, int* ic) {
+  const int side = 1 << g.hint_levels;
   const double c[3] = {p.x, p.y, p.z};
-  int idx = 0;
-  for (int k = D - 1; k >= 0; --k) {
-    double u = (c[k] - g.org[k]) * g.scale;
-    int i = (int)(u * side);
-    i = i < 0 ? 0 : (i >= side ? side - 1 : i);
-    idx = idx * side + i;
+  for (int k = 0; k < D; ++k) {
+    const double u = (c[k] - g.org[k]) * g.scale;
+    int i = u > 0.0 ? (int)fmin(u * side, (double)side) : 0;
+    ic[k] = i >= side ? side - 1 : i;
   }
+}
+template <int D>
+__device__ __forceinline__ int hint_at(const SetGeo& g, const int* ic, int level) {
+  const int sh = g.hint_levels - level;
+  int idx = 0;
+  for (int k = D - 1; k >= 0; --k) idx = (idx << level) + (ic[k] >> sh);
   const int off = D == 3 ? ((1 << (3 * level)) - 1) / 7 : ((1 << (2 * level)) - 1) / 3;
   return g.hint_off + off + idx;
 }
@@ -217,7 +226,9 @@ __device__ __forceinline__ int hint_index(const SetGeo& g, const vdp::VPt& p, in
 template <int D>
 __device__ __forceinline__ void write_hints(const DevTree& T, int vid, const vdp::VPt& q, int slot) {
   const SetGeo& g = T.sets[set_index(T, vid)];
-  for (int l = 0; l <= g.hint_levels; ++l) T.hint[hint_index<D>(g, q, l)] = slot;
+  int ic[3];
+  hint_cell<D>(g, q, ic);
+  for (int l = 0; l <= g.hint_levels; ++l) T.hint[hint_at<D>(g, ic, l)] = slot;
 }
 
 // Priority levels.  Level k holds the points with thr[k-1] <= priority <
@@ -369,7 +380,9 @@ __device__ __forceinline__ void activate_body(DevTree T, unsigned long long seed
       const vdp::VPt p = load_pt(T, vid);
       const SetGeo& g = T.sets[set_index(T, vid)];
       cur = -1;
-      for (int l = g.hint_levels; l >= 0 && cur < 0; --l) cur = T.hint[hint_index<D>(g, p, l)];
+      int ic[3];
+      hint_cell<D>(g, p, ic);
+      for (int l = g.hint_levels; l >= 0 && cur < 0; --l) cur = T.hint[hint_at<D>(g, ic, l)];
       if (cur < 0) cur = g.root;  // no insertion into the set yet: its super simplex
       int4 v, nn;
       load_simplex(T, cur, v, nn);
@@ -501,6 +514,9 @@ constexpr int kOffCN = kOffCV + 4 * kBigC;
 constexpr int kOffH = kOffCN + 4 * kBigC;
 constexpr int kOffR = kOffH + kBigH;
 constexpr int kBigInts = kOffR + 4 * kBigR;  // multiple of 4
+// Offset of the facet records after ncav cavity ids: even, so that records
+// (6 ints) start on 8-byte boundaries in an even pool stretch.
+__host__ __device__ constexpr int facets_at(int ncav) { return (ncav + 1) & ~1; }
 
 __device__ bool hset_insert(int* hk, int hs, int key) {
   unsigned h = ((unsigned)key * 2654435761u) & (hs - 1);
@@ -722,7 +738,7 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
   int mcav = 0, mfac = 0;
   // pool space is taken in per-warp chunks (one atomic per chunk, not per
   // candidate); what a warp leaves unused is dropped with the round's pool
-  const int pchunk = max(256, min(8192, T.cap_pool / (nblk * 16)));
+  const int pchunk = max(256, min(8192, T.cap_pool / (nblk * 16))) & ~1;  // offsets stay even
   int pbase = 0, pleft = 0;
   const CavStore fast{W.cav, W.cv, W.cn, W.hkey, W.fr, MAXC, MAXF, HS};
   const int nw = nblk * 4;
@@ -776,7 +792,7 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
       __syncwarp();
       continue;
     }
-    const int need = ncav + nfac * 6;
+    const int need = facets_at(ncav) + nfac * 6;
     if (need > pleft) {
       const int take = max(need, pchunk);
       if (lane == 0) pbase = atomicAdd(&T.ctr->pool_used, take);
@@ -797,7 +813,7 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
     pleft -= need;
     int* P = T.pool + off;
     for (int i = lane; i < ncav; i += 32) P[i] = W.cav[i];
-    int* F = P + ncav;
+    int* F = P + facets_at(ncav);
     for (int x = lane; x < 6 * nfac; x += 32) F[x] = W.fr[x];
     claim_region(T, W.cav, ncav, W.fr, nfac, key, lane, adjacent);
     if (lane == 0) T.cinfo[c] = make_int4(ncav, nfac, off, ST_OK);
@@ -821,7 +837,8 @@ __global__ void __launch_bounds__(128, VD_CAVITY_MIN_BLOCKS) k_cavity(DevTree T,
   cavity_body<D, XT>(T, adjacent, blockIdx.x, gridDim.x, smem); }
 
 // Pool layout of a searched candidate: cavity ids at P, facet records at
-// P + ncav, or at P + kOffF for a spilled (large) search, flagged by bit 30
+// P + facets_at(ncav) (8-byte aligned), or at P + kOffF for a spilled (large)
+// search, flagged by bit 30
 // of cinfo.y.
 __device__ __forceinline__ void cand_lists(const DevTree& T, const int4& info, int*& P, int*& F, int& ncav,
                                            int& nfac, bool& big) {
@@ -829,7 +846,7 @@ __device__ __forceinline__ void cand_lists(const DevTree& T, const int4& info, i
   ncav = info.x;
   big = (info.y >> 30) & 1;
   nfac = info.y & ((1 << 30) - 1);
-  F = big ? P + kOffF : P + ncav;
+  F = big ? P + kOffF : P + facets_at(ncav);
 }
 
 template <int D>
@@ -909,30 +926,36 @@ __device__ void write_star(const DevTree& T, WarpCommit<D>& W, const int* __rest
       W.ra[i] = -1;
     }
     __syncwarp();  // also orders the record stores above before the link stores below
-    for (int it = lane; it < nfac * NV; it += 32) {
-      const int j = it / NV, g = it - j * NV;
-      const int* r = FR + 6 * j;
+    for (int j = lane; j < nfac; j += 32) {
+      // the facet record in three 8-byte loads (records are 8-byte aligned)
+      const int2* r2 = reinterpret_cast<const int2*>(FR + 6 * j);
+      const int2 a = r2[0], b = r2[1], c = r2[2];
+      const int r[6] = {a.x, a.y, b.x, b.y, c.x, c.y};
       const int qf = r[5] & 3;
-      if (g == qf) continue;
-      int r0, r1;
-      ridge_of<D>(r, g, qf, r0, r1);
-      const unsigned hv = ridge_hash(r0, r1);
-      if (sweeps > 1 && (int)((hv & 0xffffu) % (unsigned)sweeps) != sw) continue;
-      const unsigned long long key = ((unsigned long long)(unsigned)r0 << 32) | (unsigned)r1;
-      const int mine = (j << 2) | g;
-      unsigned h = hv >> (32 - LOG_HR);
-      for (int probe = 0; probe < HR; ++probe, h = (h + 1) & (HR - 1)) {
-        const unsigned long long old = atomicCAS(&W.rk[h], EMPTY, key);
-        if (old != EMPTY && old != key) continue;
-        const int other = atomicCAS(&W.ra[h], -1, mine);
-        if (other >= 0) {
-          // second half: link both new simplices across the ridge
-          W.ra[h] = -2;
-          const int m = other >> 2, gm = other & 3;
-          reinterpret_cast<int*>(T.simp + W.id[j])[4 + g] = (W.id[m] << 2) | gm;
-          reinterpret_cast<int*>(T.simp + W.id[m])[4 + gm] = (W.id[j] << 2) | g;
+      const int idj = W.id[j];
+#pragma unroll
+      for (int g = 0; g < NV; ++g) {
+        if (g == qf) continue;
+        int r0, r1;
+        ridge_of<D>(r, g, qf, r0, r1);
+        const unsigned hv = ridge_hash(r0, r1);
+        if (sweeps > 1 && (int)((hv & 0xffffu) % (unsigned)sweeps) != sw) continue;
+        const unsigned long long key = ((unsigned long long)(unsigned)r0 << 32) | (unsigned)r1;
+        const int mine = (j << 2) | g;
+        unsigned h = hv >> (32 - LOG_HR);
+        for (int probe = 0; probe < HR; ++probe, h = (h + 1) & (HR - 1)) {
+          const unsigned long long old = atomicCAS(&W.rk[h], EMPTY, key);
+          if (old != EMPTY && old != key) continue;
+          const int other = atomicCAS(&W.ra[h], -1, mine);
+          if (other >= 0) {
+            // second half: link both new simplices across the ridge
+            W.ra[h] = -2;
+            const int m = other >> 2, gm = other & 3;
+            reinterpret_cast<int*>(T.simp + idj)[4 + g] = (W.id[m] << 2) | gm;
+            reinterpret_cast<int*>(T.simp + W.id[m])[4 + gm] = (idj << 2) | g;
+          }
+          break;
         }
-        break;
       }
     }
     __syncwarp();
