@@ -155,6 +155,40 @@ def test_split_tier_is_sound(host, oracle, dim):
 
 
 @pytest.mark.parametrize("dim", [2, 3])
+def test_split_tier_near_sphere(host, oracle, dim):
+    """Queries a relative 1e-9 .. 1e-2 off the circumsphere, at coordinate
+    scales 2^-10 .. 2^8: the first (cheap, permanent-free) bound of the
+    split tier and the tight one both certify only correct signs."""
+    H = _hl(host)
+    rng = np.random.default_rng(500 + dim)
+    certified = checked = 0
+    for trial in range(6000):
+        scale = 2.0 ** rng.uniform(-10, 8)
+        s = rng.random((dim + 1, dim)) * scale
+        o = oracle.orient(s)
+        if o == 0:
+            continue
+        if o < 0:
+            s = s[[1, 0] + list(range(2, dim + 1))]
+        # circumcentre c (least squares on the bisector system) and radius r
+        A = 2 * (s[1:] - s[0])
+        b = (s[1:] ** 2).sum(1) - (s[0] ** 2).sum()
+        c = np.linalg.solve(A, b)
+        r = np.linalg.norm(s[0] - c)
+        u = rng.normal(size=dim)
+        u /= np.linalg.norm(u)
+        eps = 10.0 ** rng.uniform(-9, -2) * rng.choice([-1.0, 1.0])
+        q = c + u * r * (1 + eps)
+        pts = np.vstack([s, q[None, :]])
+        f = H.vdh_insphere_hl(dim, _pad(pts, dim).ctypes.data_as(dp))
+        checked += 1
+        if f != 0:
+            certified += 1
+            assert f == oracle.insphere_exact(pts[: dim + 1], pts[dim + 1]), (scale, eps, pts.tolist())
+    assert checked > 5000 and certified > checked // 3
+
+
+@pytest.mark.parametrize("dim", [2, 3])
 def test_split_exit_face(host, oracle, dim):
     H = _hl(host)
     rng = np.random.default_rng(400 + dim)

@@ -937,6 +937,16 @@ VDP_HD void hl_diffs(const FPt* v, const FPt& p, float* x, float* y, float* z, f
 constexpr float kU32sq = 3.552713678800501e-15f;  // 2^-48
 
 // insphere / incircle on split coordinates: +1 / -1 certified, 0 undecided.
+//
+// Two bounds, cheap first.  The tight one is the error bound above with the
+// permanent perm (the determinant with every product replaced by its
+// magnitude).  With L = max |difference|, every |w_i| <= 3 L^2 and every
+// permanent minor <= 6 L^3 (3D; 2D: w <= 2 L^2, minor <= 2 L^2), so perm <=
+// 72 L^5 (2D: 12 L^4) and the tight relative part 28u perm (2D: 20u perm) is
+// below 2048u L^5 = 2^-13 L^5 (2D: 256u L^4 = 2^-16 L^4) with 1.5% to spare
+// for the rounding of the bound itself.  A determinant above that needs no
+// permanent at all; only the rest pays for it.  The cheap bound is used for
+// L >= 2^-12 (2D: 2^-15), where L^5 (L^4) stays far from underflow.
 template <int D>
 VDP_HD int insphere_hl(const FPt* v, const FPt& q) {
   constexpr int NV = D + 1;
@@ -945,37 +955,58 @@ VDP_HD int insphere_hl(const FPt* v, const FPt& q) {
   if (!(L <= kMax32) || !(M <= 1.152921504606847e18f)) return 0;
   if (D == 3) {
     const float abs_term = 8192.0f * kU32sq * M * (L * L) * (L * L);
-    float m01 = ffma(x[0], y[1], -(y[0] * x[1])), p01 = fabsf(x[0] * y[1]) + fabsf(y[0] * x[1]);
-    float m02 = ffma(x[0], y[2], -(y[0] * x[2])), p02 = fabsf(x[0] * y[2]) + fabsf(y[0] * x[2]);
-    float m03 = ffma(x[0], y[3], -(y[0] * x[3])), p03 = fabsf(x[0] * y[3]) + fabsf(y[0] * x[3]);
-    float m12 = ffma(x[1], y[2], -(y[1] * x[2])), p12 = fabsf(x[1] * y[2]) + fabsf(y[1] * x[2]);
-    float m13 = ffma(x[1], y[3], -(y[1] * x[3])), p13 = fabsf(x[1] * y[3]) + fabsf(y[1] * x[3]);
-    float m23 = ffma(x[2], y[3], -(y[2] * x[3])), p23 = fabsf(x[2] * y[3]) + fabsf(y[2] * x[3]);
+    float m01 = ffma(x[0], y[1], -(y[0] * x[1]));
+    float m02 = ffma(x[0], y[2], -(y[0] * x[2]));
+    float m03 = ffma(x[0], y[3], -(y[0] * x[3]));
+    float m12 = ffma(x[1], y[2], -(y[1] * x[2]));
+    float m13 = ffma(x[1], y[3], -(y[1] * x[3]));
+    float m23 = ffma(x[2], y[3], -(y[2] * x[3]));
     float D123 = ffma(z[3], m12, ffma(z[1], m23, -(z[2] * m13)));
     float D023 = ffma(z[3], m02, ffma(z[0], m23, -(z[2] * m03)));
     float D013 = ffma(z[3], m01, ffma(z[0], m13, -(z[1] * m03)));
     float D012 = ffma(z[2], m01, ffma(z[0], m12, -(z[1] * m02)));
-    float P123 = fabsf(z[1]) * p23 + fabsf(z[2]) * p13 + fabsf(z[3]) * p12;
-    float P023 = fabsf(z[0]) * p23 + fabsf(z[2]) * p03 + fabsf(z[3]) * p02;
-    float P013 = fabsf(z[0]) * p13 + fabsf(z[1]) * p03 + fabsf(z[3]) * p01;
-    float P012 = fabsf(z[0]) * p12 + fabsf(z[1]) * p02 + fabsf(z[2]) * p01;
     float w0 = ffma(z[0], z[0], ffma(y[0], y[0], x[0] * x[0]));
     float w1 = ffma(z[1], z[1], ffma(y[1], y[1], x[1] * x[1]));
     float w2 = ffma(z[2], z[2], ffma(y[2], y[2], x[2] * x[2]));
     float w3 = ffma(z[3], z[3], ffma(y[3], y[3], x[3] * x[3]));
     float det = ffma(w3, D012, ffma(-w2, D013, ffma(w1, D023, -(w0 * D123))));
+    if (L >= 2.44140625e-4f) {  // 2^-12
+      const float L2 = L * L;
+      const float cheap = 1.220703125e-4f * (L2 * L2 * L) + 1.001f * abs_term;  // 2^-13 L^5
+      if (det > cheap) return 1;
+      if (det < -cheap) return -1;
+    }
+    float p01 = fabsf(x[0] * y[1]) + fabsf(y[0] * x[1]);
+    float p02 = fabsf(x[0] * y[2]) + fabsf(y[0] * x[2]);
+    float p03 = fabsf(x[0] * y[3]) + fabsf(y[0] * x[3]);
+    float p12 = fabsf(x[1] * y[2]) + fabsf(y[1] * x[2]);
+    float p13 = fabsf(x[1] * y[3]) + fabsf(y[1] * x[3]);
+    float p23 = fabsf(x[2] * y[3]) + fabsf(y[2] * x[3]);
+    float P123 = fabsf(z[1]) * p23 + fabsf(z[2]) * p13 + fabsf(z[3]) * p12;
+    float P023 = fabsf(z[0]) * p23 + fabsf(z[2]) * p03 + fabsf(z[3]) * p02;
+    float P013 = fabsf(z[0]) * p13 + fabsf(z[1]) * p03 + fabsf(z[3]) * p01;
+    float P012 = fabsf(z[0]) * p12 + fabsf(z[1]) * p02 + fabsf(z[2]) * p01;
     float perm = w0 * P123 + w1 * P023 + w2 * P013 + w3 * P012;
     if (!(perm >= kMinPerm32)) return 0;
     return sgn_bound(det, 28.0f * kU32 * perm + abs_term);
   } else {
     const float abs_term = 1024.0f * kU32sq * M * (L * L) * L;
-    float m12 = ffma(x[1], y[2], -(y[1] * x[2])), p12 = fabsf(x[1] * y[2]) + fabsf(y[1] * x[2]);
-    float m02 = ffma(x[0], y[2], -(y[0] * x[2])), p02 = fabsf(x[0] * y[2]) + fabsf(y[0] * x[2]);
-    float m01 = ffma(x[0], y[1], -(y[0] * x[1])), p01 = fabsf(x[0] * y[1]) + fabsf(y[0] * x[1]);
+    float m12 = ffma(x[1], y[2], -(y[1] * x[2]));
+    float m02 = ffma(x[0], y[2], -(y[0] * x[2]));
+    float m01 = ffma(x[0], y[1], -(y[0] * x[1]));
     float w0 = ffma(y[0], y[0], x[0] * x[0]);
     float w1 = ffma(y[1], y[1], x[1] * x[1]);
     float w2 = ffma(y[2], y[2], x[2] * x[2]);
     float det = ffma(w2, m01, ffma(-w1, m02, w0 * m12));
+    if (L >= 3.0517578125e-5f) {  // 2^-15
+      const float L2 = L * L;
+      const float cheap = 1.52587890625e-5f * (L2 * L2) + 1.001f * abs_term;  // 2^-16 L^4
+      if (det > cheap) return 1;
+      if (det < -cheap) return -1;
+    }
+    float p12 = fabsf(x[1] * y[2]) + fabsf(y[1] * x[2]);
+    float p02 = fabsf(x[0] * y[2]) + fabsf(y[0] * x[2]);
+    float p01 = fabsf(x[0] * y[1]) + fabsf(y[0] * x[1]);
     float perm = w0 * p12 + w1 * p02 + w2 * p01;
     if (!(perm >= kMinPerm32)) return 0;
     return sgn_bound(det, 20.0f * kU32 * perm + abs_term);
