@@ -498,7 +498,9 @@ struct CavStore {
   int4* cv;     // their vertex ids
   int4* cn;     // their neighbour codes
   int* hk;      // open-addressing set of cavity ids (hs slots, power of two)
-  int* fr;      // boundary facets, 6 ints each: new simplex vertices (4), outer code, (k << 2) | face
+  int2* fr;     // boundary facets: (outer code, (k << 2) | face); expanded to
+                // 6-int records (new simplex vertices, outer code, (k << 2) | face)
+                // when the lists are stored
   int maxc, maxf, hs;
 };
 
@@ -548,8 +550,8 @@ struct WarpCtl {
 // with ctl.flags != 0 if a capacity was exceeded.
 template <int D, int XT>
 __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl, int lane, int start,
-                              int4 v0, int4 n0, int qv, const vdp::VPt& q, const vdp::FPt& fq,
-                              vdp::Tally& tl, int& perr, unsigned long long& ntests) {
+                              int4 v0, int4 n0, int qv, const vdp::FPt& fq, vdp::Tally& tl, int& perr,
+                              unsigned long long& ntests) {
   constexpr int NV = D + 1;
   for (int i = lane; i < S.hs; i += 32) S.hk[i] = -1;
   if (lane == 0) {
@@ -593,7 +595,7 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
           ++ntests;
           auto load64 = [&](vdp::VPt* v64, vdp::VPt& q64) {
             for (int j = 0; j < NV; ++j) v64[j] = load_pt(T, kv[j]);
-            q64 = q;
+            q64 = load_pt(T, qv);  // reloaded: the rare FP64 path need not hold q in registers
           };
           if (vdp::in_conflict_hl<D, XT>(fv, kv, fq, qv, tl, perr, load64)) {
             if (hset_insert(S.hk, S.hs, nb)) {
@@ -614,14 +616,7 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
       if (facet) {
         int s = atomicAdd(&ctl.nfac, 1);
         if (s < S.maxf) {
-          const int4 nv4 = set4(S.cv[k], f, qv);
-          int* r = S.fr + 6 * s;
-          r[0] = nv4.x;
-          r[1] = nv4.y;
-          r[2] = nv4.z;
-          r[3] = nv4.w;
-          r[4] = code;
-          r[5] = (k << 2) | f;
+          S.fr[s] = make_int2(code, (k << 2) | f);
         } else {
           atomicOr(&ctl.flags, 2);
         }
@@ -709,12 +704,26 @@ struct WarpCav {
   int4 cv[Cap<D>::MAXC];
   int4 cn[Cap<D>::MAXC];
   int hkey[Cap<D>::HS];
-  int fr[6 * Cap<D>::MAXF];
+  int2 fr[Cap<D>::MAXF];
 };
 
 // Claims of a candidate for one resolution pass: its cavity in claim_c, every
 // outer neighbour in claim_n (not in adjacent mode, where cavities may touch).
 // P = cavity ids, F = facet records.
+// Facet records of a search, expanded for the later kernels: the new
+// simplex on facet (k, f) has the vertices of cavity simplex k with v[f]
+// replaced by the candidate's point qv.
+__device__ __forceinline__ void expand_facets(const int2* fr, const int4* cv, int nfac, int qv, int* F, int lane) {
+  for (int j = lane; j < nfac; j += 32) {
+    const int2 e = fr[j];
+    const int4 nv4 = set4(cv[e.y >> 2], e.y & 3, qv);
+    int2* r = reinterpret_cast<int2*>(F + 6 * j);  // records start on 8-byte boundaries
+    r[0] = make_int2(nv4.x, nv4.y);
+    r[1] = make_int2(nv4.z, nv4.w);
+    r[2] = e;
+  }
+}
+
 __device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int ncav, const int* F,
                                              int nfac, unsigned long long key, int lane, int adjacent) {
   for (int i = lane; i < ncav; i += 32) atomicMin(T.claim_c + P[i], key);
@@ -746,13 +755,12 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
   for (int it = bid * 4 + wib; it < nsurv; it += nw) {
     const int c = T.wl[0][it];
     const int4 cd = T.cand[c];
-    const vdp::VPt q = load_pt(T, cd.x);
     const vdp::FPt fq = load_fpt(T, cd.x);
     int4 v0, n0;
     load_simplex(T, cd.y, v0, n0);
     if (lane == 0) ++nsearched;
     const unsigned long long key = pe | (unsigned)cd.z;
-    cavity_search<D, XT>(T, fast, W.ctl, lane, cd.y, v0, n0, cd.x, q, fq, tl, perr, ntests);
+    cavity_search<D, XT>(T, fast, W.ctl, lane, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
     int ncav = min(W.ctl.ncav, MAXC), nfac = min(W.ctl.nfac, MAXF);
     int off = 0;
     if (W.ctl.flags) {
@@ -771,9 +779,11 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
         continue;
       }
       int* P = T.pool + off;
+      // the search's 2-int facet records go to the ridge-table area (unused
+      // until the commit) and are expanded to P + kOffF afterwards
       const CavStore big{P, reinterpret_cast<int4*>(P + kOffCV), reinterpret_cast<int4*>(P + kOffCN),
-                         P + kOffH, P + kOffF, kBigC, kBigF, kBigH};
-      cavity_search<D, XT>(T, big, W.ctl, lane, cd.y, v0, n0, cd.x, q, fq, tl, perr, ntests);
+                         P + kOffH, reinterpret_cast<int2*>(P + kOffR), kBigC, kBigF, kBigH};
+      cavity_search<D, XT>(T, big, W.ctl, lane, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
       if (W.ctl.flags) {
         if (lane == 0) {
           T.cinfo[c] = make_int4(W.ctl.ncav, W.ctl.nfac, 0, ST_OVERFLOW);
@@ -785,6 +795,8 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
       ncav = W.ctl.ncav;
       nfac = W.ctl.nfac;
       // the facets stay at P + kOffF; cinfo.y carries the flag (see below)
+      expand_facets(big.fr, big.cv, nfac, cd.x, P + kOffF, lane);
+      __syncwarp();
       claim_region(T, P, ncav, P + kOffF, nfac, key, lane, adjacent);
       if (lane == 0) T.cinfo[c] = make_int4(ncav, nfac | (1 << 30), off, ST_OK);
       mcav = max(mcav, ncav);
@@ -814,8 +826,9 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
     int* P = T.pool + off;
     for (int i = lane; i < ncav; i += 32) P[i] = W.cav[i];
     int* F = P + facets_at(ncav);
-    for (int x = lane; x < 6 * nfac; x += 32) F[x] = W.fr[x];
-    claim_region(T, W.cav, ncav, W.fr, nfac, key, lane, adjacent);
+    expand_facets(W.fr, W.cv, nfac, cd.x, F, lane);
+    __syncwarp();
+    claim_region(T, W.cav, ncav, F, nfac, key, lane, adjacent);
     if (lane == 0) T.cinfo[c] = make_int4(ncav, nfac, off, ST_OK);
     mcav = max(mcav, ncav);
     mfac = max(mfac, nfac);
