@@ -48,3 +48,22 @@ def test_exact_tier_arg_errors(vd):
         t.set_exact_tier(3)
     with pytest.raises(vd.VDError):
         t.set_exact_tier(0, -1)
+
+
+@pytest.mark.parametrize("small_rounds", [0, 1 << 30])
+def test_large_regions_block_search(vd, oracle, small_rounds):
+    """Near-degenerate points whose conflict regions outgrow a warp's shared
+    memory: the searches are redone in the pool, by a whole block
+    (k_cavity_big) in the default path and by the warp inside the
+    cooperative small-round kernel.  Same edges as the oracle either way."""
+    p = W.c3_points(n=60000)
+    t = vd.DelaunayTree(p)
+    t.set_small_rounds(small_rounds)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", RuntimeWarning)
+        t.add_points_to_tree(p, seed=5)
+    st = t.stats()
+    assert st["spilled"] > 0 and st["max_cavity"] > 128
+    ok, det = t.check_delaunay(details=True)
+    assert ok, det
+    assert np.array_equal(t.edges(), oracle.Triangulation(p, seed=5).edges())

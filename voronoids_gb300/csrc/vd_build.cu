@@ -548,12 +548,23 @@ struct WarpCtl {
 // Breadth-first search of the conflict region of candidate q from the
 // simplex that contains it; all 32 lanes of the warp call this.  Returns
 // with ctl.flags != 0 if a capacity was exceeded.
-template <int D, int XT>
+//
+// BLOCK: the whole block searches (k_cavity_big, lane = thread index, waves
+// of blockDim.x items); ctl.pad carries the wave's item count, published by
+// thread 0 so that every thread leaves the loop after the same barrier.
+template <int D, int XT, bool BLOCK = false>
 __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl, int lane, int start,
                               int4 v0, int4 n0, int qv, const vdp::FPt& fq, vdp::Tally& tl, int& perr,
                               unsigned long long& ntests) {
   constexpr int NV = D + 1;
-  for (int i = lane; i < S.hs; i += 32) S.hk[i] = -1;
+  const int G = BLOCK ? (int)blockDim.x : 32;
+  auto sync = [] {
+    if (BLOCK)
+      __syncthreads();
+    else
+      __syncwarp();
+  };
+  for (int i = lane; i < S.hs; i += G) S.hk[i] = -1;
   if (lane == 0) {
     ctl.ncav = 1;
     ctl.nfac = 0;
@@ -562,17 +573,28 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
     S.cv[0] = v0;
     S.cn[0] = n0;
   }
-  __syncwarp();
+  sync();
   if (lane == 0) hset_insert(S.hk, S.hs, start);
-  __syncwarp();
-  // (simplex, face) items are taken in waves of 32 in discovery order, not
+  sync();
+  // (simplex, face) items are taken in waves of G in discovery order, not
   // level by level: a wave also takes the items of simplices the previous
-  // wave appended, so a search needs about items / 32 dependent rounds of
+  // wave appended, so a search needs about items / G dependent rounds of
   // gathers rather than one or more per level
   int head = 0, levels = 0;
   while (true) {
-    const int avail = min(*(volatile int*)&ctl.ncav, S.maxc) * NV;
-    if (*(volatile int*)&ctl.flags || head >= avail) break;
+    int avail;
+    if (BLOCK) {
+      if (lane == 0) {
+        const int a = min(*(volatile int*)&ctl.ncav, S.maxc) * NV;
+        ctl.pad = (*(volatile int*)&ctl.flags || head >= a) ? -1 : a;
+      }
+      sync();
+      avail = *(volatile int*)&ctl.pad;
+      if (avail < 0) break;
+    } else {
+      avail = min(*(volatile int*)&ctl.ncav, S.maxc) * NV;
+      if (*(volatile int*)&ctl.flags || head >= avail) break;
+    }
     ++levels;
     const int it = head + lane;
     if (it < avail) {
@@ -622,10 +644,10 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
         }
       }
     }
-    __syncwarp();
-    head += min(32, avail - head);
+    sync();
+    head += min(G, avail - head);
   }
-  __syncwarp();
+  sync();
   if (lane == 0 && levels > 64) atomicMax(&T.ctr->max_levels, levels);
 }
 
@@ -734,8 +756,78 @@ __device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int
   }
 }
 
+// Search of a conflict region too large for a warp's shared memory, with
+// its lists in a reserved stretch of the round's pool (global memory); a
+// warp (BLOCK = false) or the whole block (k_cavity_big) runs it.  The
+// stretch offset is broadcast through ctl.pad.
+template <int D, int XT, bool BLOCK>
+__device__ void big_search(const DevTree& T, WarpCtl& ctl, int rank, int c, int4 cd, int4 v0, int4 n0,
+                           const vdp::FPt& fq, unsigned long long key, int adjacent, vdp::Tally& tl, int& perr,
+                           unsigned long long& ntests, int& mcav, int& mfac) {
+  auto sync = [] {
+    if (BLOCK)
+      __syncthreads();
+    else
+      __syncwarp();
+  };
+  if (rank == 0) {
+    const int o = atomicAdd(&T.ctr->pool_used, kBigInts + 4);
+    ctl.pad = (o + 3) & ~3;  // int4 alignment of cv / cn
+  }
+  sync();
+  const int off = *(volatile int*)&ctl.pad;
+  sync();
+  if (off + kBigInts > T.cap_pool) {
+    if (rank == 0) {
+      T.cinfo[c] = make_int4(0, 0, 0, ST_POOL);
+      atomicAdd(&T.ctr->pool_overflow, 1);
+    }
+    sync();
+    return;
+  }
+  int* P = T.pool + off;
+  // the search's 2-int facet records go to the ridge-table area (unused
+  // until the commit) and are expanded to P + kOffF afterwards
+  const CavStore big{P, reinterpret_cast<int4*>(P + kOffCV), reinterpret_cast<int4*>(P + kOffCN),
+                     P + kOffH, reinterpret_cast<int2*>(P + kOffR), kBigC, kBigF, kBigH};
+  cavity_search<D, XT, BLOCK>(T, big, ctl, rank, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
+  const int ncav = *(volatile int*)&ctl.ncav, nfac = *(volatile int*)&ctl.nfac;
+  const int flags = *(volatile int*)&ctl.flags;
+  sync();
+  if (flags) {
+    if (rank == 0) {
+      T.cinfo[c] = make_int4(ncav, nfac, 0, ST_OVERFLOW);
+      atomicAdd(&T.ctr->overflow, 1);
+    }
+    sync();
+    return;
+  }
+  // the facets stay at P + kOffF; cinfo.y carries the flag (see cand_lists)
+  const int G = BLOCK ? (int)blockDim.x : 32;
+  for (int j = rank; j < nfac; j += G) {
+    const int2 e = big.fr[j];
+    const int4 nv4 = set4(big.cv[e.y >> 2], e.y & 3, cd.x);
+    int2* r = reinterpret_cast<int2*>(P + kOffF + 6 * j);
+    r[0] = make_int2(nv4.x, nv4.y);
+    r[1] = make_int2(nv4.z, nv4.w);
+    r[2] = e;
+  }
+  sync();
+  for (int i = rank; i < ncav; i += G) atomicMin(T.claim_c + P[i], key);
+  if (!adjacent)
+    for (int j = rank; j < nfac; j += G) {
+      const int o = P[kOffF + 6 * j + 4];
+      if (o >= 0 && !bad_simp(T, o >> 2)) atomicMin(T.claim_n + (o >> 2), key);
+    }
+  if (rank == 0) T.cinfo[c] = make_int4(ncav, nfac | (1 << 30), off, ST_OK);
+  mcav = max(mcav, ncav);
+  mfac = max(mfac, nfac);
+  sync();
+}
+
 template <int D, int XT>
-__device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, int nblk, WarpCav<D>* smem) {
+__device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, int nblk, WarpCav<D>* smem,
+                                            bool defer_big) {
   const int round = T.ctr->round;
   constexpr int MAXC = Cap<D>::MAXC, MAXF = Cap<D>::MAXF, HS = Cap<D>::HS;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -764,43 +856,17 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
     int ncav = min(W.ctl.ncav, MAXC), nfac = min(W.ctl.nfac, MAXF);
     int off = 0;
     if (W.ctl.flags) {
-      // spill: redo the search with its lists in a reserved pool stretch
-      if (lane == 0) {
-        ++nspill;
-        off = atomicAdd(&T.ctr->pool_used, kBigInts + 4);
-      }
-      off = (__shfl_sync(FULL, off, 0) + 3) & ~3;  // int4 alignment of cv / cn
-      if (off + kBigInts > T.cap_pool) {
+      // spill: the region outgrew shared memory; the search is redone in a
+      // reserved pool stretch, by the whole block of k_cavity_big or here
+      if (lane == 0) ++nspill;
+      if (defer_big) {
         if (lane == 0) {
-          T.cinfo[c] = make_int4(0, 0, 0, ST_POOL);
-          atomicAdd(&T.ctr->pool_overflow, 1);
+          T.bigc[atomicAdd(&T.ctr->nbig, 1)] = c;
+          T.cinfo[c] = make_int4(0, 0, 0, ST_BIG);
         }
-        __syncwarp();
-        continue;
+      } else {
+        big_search<D, XT, false>(T, W.ctl, lane, c, cd, v0, n0, fq, key, adjacent, tl, perr, ntests, mcav, mfac);
       }
-      int* P = T.pool + off;
-      // the search's 2-int facet records go to the ridge-table area (unused
-      // until the commit) and are expanded to P + kOffF afterwards
-      const CavStore big{P, reinterpret_cast<int4*>(P + kOffCV), reinterpret_cast<int4*>(P + kOffCN),
-                         P + kOffH, reinterpret_cast<int2*>(P + kOffR), kBigC, kBigF, kBigH};
-      cavity_search<D, XT>(T, big, W.ctl, lane, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
-      if (W.ctl.flags) {
-        if (lane == 0) {
-          T.cinfo[c] = make_int4(W.ctl.ncav, W.ctl.nfac, 0, ST_OVERFLOW);
-          atomicAdd(&T.ctr->overflow, 1);
-        }
-        __syncwarp();
-        continue;
-      }
-      ncav = W.ctl.ncav;
-      nfac = W.ctl.nfac;
-      // the facets stay at P + kOffF; cinfo.y carries the flag (see below)
-      expand_facets(big.fr, big.cv, nfac, cd.x, P + kOffF, lane);
-      __syncwarp();
-      claim_region(T, P, ncav, P + kOffF, nfac, key, lane, adjacent);
-      if (lane == 0) T.cinfo[c] = make_int4(ncav, nfac | (1 << 30), off, ST_OK);
-      mcav = max(mcav, ncav);
-      mfac = max(mfac, nfac);
       __syncwarp();
       continue;
     }
@@ -846,8 +912,38 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
   }
 }
 template <int D, int XT>
-__global__ void __launch_bounds__(128, VD_CAVITY_MIN_BLOCKS) k_cavity(DevTree T, int adjacent) { __shared__ WarpCav<D> smem[4];
-  cavity_body<D, XT>(T, adjacent, blockIdx.x, gridDim.x, smem); }
+__global__ void __launch_bounds__(128, VD_CAVITY_MIN_BLOCKS) k_cavity(DevTree T, int adjacent, int defer_big) {
+  __shared__ WarpCav<D> smem[4];
+  cavity_body<D, XT>(T, adjacent, blockIdx.x, gridDim.x, smem, defer_big != 0);
+}
+
+// The searches k_cavity deferred (ST_BIG): one block per search, waves of
+// 512 (simplex, face) items.
+template <int D, int XT>
+__global__ void __launch_bounds__(512, 1) k_cavity_big(DevTree T, int adjacent) {
+  __shared__ WarpCtl ctl;
+  const int n = T.ctr->nbig;
+  if (n == 0) return;
+  const unsigned long long pe = pass_epoch(T.ctr->round, 0);
+  vdp::Tally tl = {0, 0, 0, 0};
+  int perr = 0, mcav = 0, mfac = 0;
+  unsigned long long ntests = 0;
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const int c = T.bigc[i];
+    const int4 cd = T.cand[c];
+    const vdp::FPt fq = load_fpt(T, cd.x);
+    int4 v0, n0;
+    load_simplex(T, cd.y, v0, n0);
+    big_search<D, XT, true>(T, ctl, threadIdx.x, c, cd, v0, n0, fq, pe | (unsigned)cd.z, adjacent, tl, perr, ntests,
+                            mcav, mfac);
+  }
+  if (perr) set_error(T.ctr, E_PRECISION);
+  flush_tally(T.ctr, tl, ntests, 0);
+  if (threadIdx.x == 0) {
+    if (mcav) atomicMax(&T.ctr->max_cav, mcav);
+    if (mfac) atomicMax(&T.ctr->max_fac, mfac);
+  }
+}
 
 // Pool layout of a searched candidate: cavity ids at P, facet records at
 // P + facets_at(ncav) (8-byte aligned), or at P + kOffF for a spilled (large)
@@ -981,15 +1077,23 @@ __device__ void write_star(const DevTree& T, WarpCommit<D>& W, const int* __rest
 
 // Star of one winner, large case: every (facet, face) inserts its ridge into
 // an open-addressing table (two halves per ridge), then reads its partner.
-template <int D>
+// A warp (BLOCK = false) or the whole block (k_commit_big) writes it.
+template <int D, bool BLOCK = false>
 __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, int nfac, int round,
                                int* R, int lane) {
   constexpr int NV = D + 1;
+  const int G = BLOCK ? (int)blockDim.x : 32;
+  auto sync = [] {
+    if (BLOCK)
+      __syncthreads();
+    else
+      __syncwarp();
+  };
   const unsigned mask = kBigR - 1;
-  for (int i = lane; i < 4 * kBigR; i += 32) R[i] = -1;
-  __syncwarp();
+  for (int i = lane; i < 4 * kBigR; i += G) R[i] = -1;
+  sync();
   // R[4h] = r0, R[4h+1] = r1 (key), R[4h+2], R[4h+3] = the two half-ridges
-  for (int it = lane; it < nfac * NV; it += 32) {
+  for (int it = lane; it < nfac * NV; it += G) {
     const int j = it / NV, g = it - j * NV;
     const int* r = FR + 6 * j;
     const int qf = r[5] & 3;
@@ -1010,8 +1114,8 @@ __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, i
       }
     }
   }
-  __syncwarp();
-  for (int j = lane; j < nfac; j += 32) {
+  sync();
+  for (int j = lane; j < nfac; j += G) {
     const int* r = FR + 6 * j;
     const int qf = r[5] & 3;
     int4 nn = make_int4(-1, -1, -1, -1);
@@ -1043,6 +1147,26 @@ __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, i
     }
     emit_simplex(T, r, ID[j], nn, round);
   }
+  sync();
+}
+
+// Adjacent mode, commit half of a large star after its links: facets shared
+// with another winner's cavity publish this side's new simplex and record
+// where the other side's goes (fix_body).
+template <bool BLOCK>
+__device__ __forceinline__ void publish_shared_facets(const DevTree& T, int* F, const int* P, const int* IDS,
+                                                      int nfac, int round, int lane) {
+  const int G = BLOCK ? (int)blockDim.x : 32;
+  for (int j = lane; j < nfac; j += G) {
+    const int o = F[6 * j + 4];
+    if (o < 0 || bad_simp(T, o >> 2) || T.killed[o >> 2].x != round) continue;
+    const int kf = F[6 * j + 5], k = kf >> 2;
+    const int inner = (P[k] << 2) | (kf & 3);  // the removed simplex and its face on this facet
+    T.repl[inner] = (IDS[j] << 2) | (kf & 3);
+    F[6 * j] = IDS[j];
+    F[6 * j + 1] = kf & 3;
+    F[6 * j + 2] = -2;
+  }
 }
 
 // Resolution pass `pass` of a round, check half.  A candidate wins iff it
@@ -1070,9 +1194,10 @@ __device__ void write_star_big(const DevTree& T, const int* FR, const int* ID, i
 // simplex removed in the pass and leaves links into them to fix_body.
 template <int D, int MODE, int XT>
 __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsigned long long seed, int bid, int nblk,
-                                           unsigned char* dsm) {
+                                           unsigned char* dsm, bool defer_big = false) {
   constexpr int NV = D + 1;
   const int round = T.ctr->round;
+  if (MODE == 1 && bid == 0 && threadIdx.x == 0) T.ctr->nbigw = 0;  // stars deferred by this pass's commit
   const int sin = 2 * pass, sout = 2 * pass + 1;
   constexpr int MAXF = Cap<D>::MAXF, MAXC = Cap<D>::MAXC;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1236,7 +1361,13 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
       } else {
         // large star (spilled search): plain slot assignment, ids in the
         // stretch's vertex-list area (free after the search), ridge table in
-        // its own area
+        // its own area; with defer_big the whole block of k_commit_big
+        // writes it (and the rest of this winner's commit)
+        if (MODE == 2 && defer_big) {
+          if (lane == 0) T.bigw[atomicAdd(&T.ctr->nbigw, 1)] = c;
+          __syncwarp();
+          continue;
+        }
         int* ID = P + kOffCV;
         for (int j = lane; j < nfac; j += 32) ID[j] = j < ncav ? P[j] : base + (j - ncav);
         __syncwarp();
@@ -1250,17 +1381,7 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
         // facets shared with another winner's cavity: publish this side's new
         // simplex and remember where the other side's goes (fix_body)
         __syncwarp();
-        for (int j = lane; j < nfac; j += 32) {
-          const int o = F[6 * j + 4];
-          if (o < 0 || bad_simp(T, o >> 2) || T.killed[o >> 2].x != round) continue;
-          const int kf = F[6 * j + 5], qf = kf & 3, k = kf >> 2;
-          const int inner = (P[k] << 2) | (kf & 3);  // the removed simplex and its face on this facet
-          (void)qf;
-          T.repl[inner] = (IDS[j] << 2) | (kf & 3);
-          F[6 * j] = IDS[j];
-          F[6 * j + 1] = kf & 3;
-          F[6 * j + 2] = -2;
-        }
+        publish_shared_facets<false>(T, F, P, IDS, nfac, round, lane);
       }
       if (lane == 0) {
         write_hints<D>(T, cd.x, load_pt(T, cd.x), id0);
@@ -1290,8 +1411,53 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
   }
 }
 template <int D, int MODE, int XT>
-__global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last, unsigned long long seed) { extern __shared__ __align__(16) unsigned char dsm[];
-  check_body<D, MODE, XT>(T, pass, last, seed, blockIdx.x, gridDim.x, dsm); }
+__global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last, unsigned long long seed, int defer_big) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  check_body<D, MODE, XT>(T, pass, last, seed, blockIdx.x, gridDim.x, dsm, defer_big != 0);
+}
+
+// The large stars the commit half deferred: one block per winner writes its
+// star, publishes its shared facets and its hints.
+template <int D>
+__global__ void __launch_bounds__(512, 1) k_commit_big(DevTree T) {
+  const int n = T.ctr->nbigw;
+  if (n == 0) return;
+  const int round = T.ctr->round;
+  const int par = round & 1;
+  unsigned long long ncreated = 0, nkilled = 0;
+  int nholes = 0;
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const int c = T.bigw[i];
+    const int4 info = T.cinfo[c];
+    const int4 cd = T.cand[c];
+    int *P, *F, ncav, nfac;
+    bool big;
+    cand_lists(T, info, P, F, ncav, nfac, big);
+    const int base = cd.y;
+    int* ID = P + kOffCV;
+    for (int j = threadIdx.x; j < nfac; j += blockDim.x) ID[j] = j < ncav ? P[j] : base + (j - ncav);
+    __syncthreads();
+    const int id0 = ID[0];
+    for (int k = nfac + threadIdx.x; k < ncav; k += blockDim.x)
+      store_simplex(T, P[k], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
+    write_star_big<D, true>(T, F, ID, nfac, round, P + kOffR, threadIdx.x);
+    publish_shared_facets<true>(T, F, P, ID, nfac, round, threadIdx.x);
+    if (threadIdx.x == 0) {
+      write_hints<D>(T, cd.x, load_pt(T, cd.x), id0);
+      T.cinfo[c].w = ST_DONE;
+      T.act[par][cd.w].x = -1;
+    }
+    ncreated += nfac;
+    nkilled += ncav;
+    nholes += max(0, ncav - nfac);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && ncreated) {
+    atomicAdd(&T.ctr->created, ncreated);
+    atomicAdd(&T.ctr->killed, nkilled);
+    if (nholes) atomicAdd(&T.ctr->holes, nholes);
+  }
+}
 
 // Adjacent mode, end of a round: a new simplex whose outer neighbour another
 // winner removed takes, as that neighbour, the other winner's new simplex on
@@ -1376,6 +1542,7 @@ __device__ __forceinline__ void relocate_body(DevTree T, int bid, int nblk) {
   if (bid == 0 && threadIdx.x == 0) {
     T.ctr->ncand = 0;
     T.ctr->pool_used = 0;
+    T.ctr->nbig = 0;
   }
   const int n = T.ctr->nact[par];
   const unsigned long long ep1 = epoch(round + 1);
@@ -1496,7 +1663,7 @@ __global__ void __launch_bounds__(128) k_rounds_small(DevTree T, Tuning tu, unsi
     if (!grid_sync(c, nblk)) return;
     thin_body<D>(T, tu.thin, bid, nblk);
     if (!grid_sync(c, nblk)) return;
-    cavity_body<D, 0>(T, tu.adjacent, bid, nblk, reinterpret_cast<WarpCav<D>*>(dsm));
+    cavity_body<D, 0>(T, tu.adjacent, bid, nblk, reinterpret_cast<WarpCav<D>*>(dsm), false);
     if (!grid_sync(c, nblk)) return;
     for (int p = 0; p < tu.passes; ++p) {
       const int last = p == tu.passes - 1;
@@ -1536,6 +1703,8 @@ constexpr size_t small_rounds_smem() {
 // of the commit half (MODE 2), 2D and 3D.
 int g_check_wave[2] = {1 << 20, 1 << 20};
 int g_commit_wave[2] = {1 << 20, 1 << 20};
+// Grid of k_cavity_big: one 512-thread block per SM.
+int g_big_grid = 1;
 // Grid of the small-round kernel (0: not available).
 int g_small_grid[2] = {0, 0};
 
@@ -1548,7 +1717,8 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
     }
   };
   if (pf && pf->n == 0) cudaEventRecord(pf->ev[0], L.stream);
-  note_launches(tu.adjacent ? 6 + 3 * tu.passes - 1 : 6 + 2 * tu.passes - 1);
+  note_launches((tu.adjacent ? 6 + 3 * tu.passes - 1 : 6 + 2 * tu.passes - 1) +
+                (tu.big_block ? 1 + (tu.adjacent ? tu.passes : 0) : 0));
   k_plan<<<1, 32, 0, L.stream>>>(T, fd.ratio);
   k_activate<D><<<L.blocks, 256, 0, L.stream>>>(T, fd.seed);
   mark(KT_ACTIVATE);
@@ -1559,10 +1729,19 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
   // kernels with conflict tests come in two forms: exact tier on expansions
   // alone (small register allocation) or integer tier first (tu.exact_int)
   if (tu.exact_int)
-    k_cavity<D, 1><<<L.warps / 4, 128, 0, L.stream>>>(T, tu.adjacent);
+    k_cavity<D, 1><<<L.warps / 4, 128, 0, L.stream>>>(T, tu.adjacent, tu.big_block);
   else
-    k_cavity<D, 0><<<L.warps / 4, 128, 0, L.stream>>>(T, tu.adjacent);
+    k_cavity<D, 0><<<L.warps / 4, 128, 0, L.stream>>>(T, tu.adjacent, tu.big_block);
   mark(KT_CAVITY);
+  // with big_block, searches that outgrew a warp's shared memory are redone
+  // by whole blocks (the host turns it on once a call has spilled searches)
+  if (tu.big_block) {
+    if (tu.exact_int)
+      k_cavity_big<D, 1><<<g_big_grid, 512, 0, L.stream>>>(T, tu.adjacent);
+    else
+      k_cavity_big<D, 0><<<g_big_grid, 512, 0, L.stream>>>(T, tu.adjacent);
+    mark(KT_BIG);
+  }
   // the commit half needs little shared memory per warp and few registers,
   // so it runs up to twice the warps of the search (one resident wave)
   const int commit_grid = std::min(L.warps / 2, g_commit_wave[D - 2]);
@@ -1575,17 +1754,24 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
     }
     if (tu.adjacent) {
       if (tu.exact_int)
-        k_check<D, 1, 1><<<L.warps / 4, 128, 4 * sizeof(HeadBuf), L.stream>>>(T, p, last, fd.seed);
+        k_check<D, 1, 1><<<L.warps / 4, 128, 4 * sizeof(HeadBuf), L.stream>>>(T, p, last, fd.seed, 0);
       else
-        k_check<D, 1, 0><<<L.warps / 4, 128, 4 * sizeof(HeadBuf), L.stream>>>(T, p, last, fd.seed);
+        k_check<D, 1, 0><<<L.warps / 4, 128, 4 * sizeof(HeadBuf), L.stream>>>(T, p, last, fd.seed, 0);
       mark(KT_DECIDE);
-      k_check<D, 2, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
-    } else if (tu.exact_int) {
-      k_check<D, 0, 1><<<strict_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
+      k_check<D, 2, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed,
+                                                                                  tu.big_block);
+      mark(KT_CHECK);
+      if (tu.big_block) {
+        k_commit_big<D><<<g_big_grid, 512, 0, L.stream>>>(T);
+        mark(KT_BIGW);
+      }
     } else {
-      k_check<D, 0, 0><<<strict_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed);
+      if (tu.exact_int)
+        k_check<D, 0, 1><<<strict_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed, 0);
+      else
+        k_check<D, 0, 0><<<strict_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed, 0);
+      mark(KT_CHECK);
     }
-    mark(KT_CHECK);
   }
   k_relocate<D><<<L.blocks, 256, 0, L.stream>>>(T);
   mark(KT_RELOCATE);
@@ -1639,6 +1825,7 @@ int prepare_once() {
     return E_CUDA;
   g_check_wave[1] = std::max(1, sms * b3);
   g_check_wave[0] = std::max(1, sms * b2);
+  g_big_grid = std::max(1, sms);
   g_commit_wave[1] = std::max(1, sms * c3);
   g_commit_wave[0] = std::max(1, sms * c2);
   // small-round kernel: one block per SM when a block fits
@@ -1697,6 +1884,7 @@ void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, 
 
 const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_thin",     "k_cavity", "k_check",
                                                 "k_reclaim",  "k_relocate", "k_activate", "edges",
-                                                "k_decide",   "k_fix_links", "k_rounds_small"};
+                                                "k_decide",   "k_fix_links", "k_rounds_small", "k_cavity_big",
+                                                "k_commit_big"};
 
 }  // namespace vd

@@ -168,7 +168,7 @@ struct vd_tree {
   // bakes in (the device tree by value, grid, tuning and feed)
   struct ChunkGraph {
     vd::DevTree T;
-    int chunk, blocks, warps, passes, thin, adjacent, exact_int;
+    int chunk, blocks, warps, passes, thin, adjacent, exact_int, big_block;
     uint64_t seed;
     float ratio;
     long long launches;
@@ -341,9 +341,11 @@ int ensure_points(vd_tree* t, int64_t n_new) {
     dfree(t->T.wl[1]);
     dfree(t->T.order);
     dfree(t->T.win);
+    dfree(t->T.bigc);
+    dfree(t->T.bigw);
     if (dalloc(&t->T.act[0], c) || dalloc(&t->T.act[1], c) || dalloc(&t->T.cand, c) ||
         dalloc(&t->T.cinfo, c) || dalloc(&t->T.wl[0], c) || dalloc(&t->T.wl[1], c) ||
-        dalloc(&t->T.order, c) || dalloc(&t->T.win, c))
+        dalloc(&t->T.order, c) || dalloc(&t->T.win, c) || dalloc(&t->T.bigc, c) || dalloc(&t->T.bigw, c))
       return vd::E_NOMEM;
     t->cap_act = c;
     t->T.cap_cand = (int)c;
@@ -396,6 +398,8 @@ void release(vd_tree* t) {
   dfree(t->T.act[1]);
   dfree(t->T.order);
   dfree(t->T.win);
+  dfree(t->T.bigc);
+  dfree(t->T.bigw);
   dfree(t->T.repl);
   dfree(t->T.cand);
   dfree(t->T.cinfo);
@@ -707,6 +711,7 @@ bool launch_chunk_graph(vd_tree* t, const vd::Launch& L, int chunk, const vd::Fe
   for (auto& g : t->graphs)
     if (g.chunk == chunk && g.blocks == L.blocks && g.warps == L.warps && g.passes == t->tuning.passes &&
         g.thin == t->tuning.thin && g.adjacent == t->tuning.adjacent && g.exact_int == t->tuning.exact_int &&
+        g.big_block == t->tuning.big_block &&
         g.seed == fd.seed && g.ratio == fd.ratio &&
         memcmp(&g.T, &t->T, sizeof(vd::DevTree)) == 0) {
       hit = &g;
@@ -740,6 +745,7 @@ bool launch_chunk_graph(vd_tree* t, const vd::Launch& L, int chunk, const vd::Fe
     g.thin = t->tuning.thin;
     g.adjacent = t->tuning.adjacent;
     g.exact_int = t->tuning.exact_int;
+    g.big_block = t->tuning.big_block;
     g.seed = fd.seed;
     g.ratio = fd.ratio;
     g.launches = launches;
@@ -775,6 +781,10 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
   // exact tests of this call so far decide the form of the conflict-test kernels
   const unsigned long long exact0 = h.tally[2];
   bool exact_int = t->exact_mode == 2;
+  // oversized searches and stars go to whole-block kernels once the call has
+  // had one (until then a warp redoes them, and the extra kernels are not run)
+  const unsigned long long spilled0 = h.spilled;
+  bool big_block = false;
   // the first rounds, while few points are active, run in one cooperative
   // launch (k_rounds_small); the rest as chunks of captured rounds
   bool small = t->small_rounds_max > 0 && !t->trace;
@@ -785,6 +795,7 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
     const vd::Feed& fd = early ? fd_early : fd_main;
     t->tuning = early ? tu_early : tu_main;
     t->tuning.exact_int = exact_int ? 1 : 0;
+    t->tuning.big_block = big_block ? 1 : 0;
     bool ran_small = false;
     if (small) {
       small = false;
@@ -831,6 +842,7 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
       break;
     }
     if (t->exact_mode == 0 && (int64_t)(h.tally[2] - exact0) >= t->exact_switch) exact_int = true;
+    if (h.spilled > spilled0) big_block = true;
     active = h.nact[r & 1];
     fed = h.feed_hi;
     done = h.ninserted;

@@ -36,7 +36,8 @@ struct alignas(32) Simplex {
 };
 
 // Per-round statuses of a candidate.
-enum : int { ST_OK = 0, ST_DUP = 1, ST_OVERFLOW = 2, ST_POOL = 3, ST_LOST = 4, ST_DONE = 5, ST_WIN = 6 };
+// ST_BIG: the search outgrew a warp's shared memory and waits for k_cavity_big.
+enum : int { ST_OK = 0, ST_DUP = 1, ST_OVERFLOW = 2, ST_POOL = 3, ST_LOST = 4, ST_DONE = 5, ST_WIN = 6, ST_BIG = 7 };
 
 // Resolution passes per round (independent-set refinement), see vd_build.cu.
 constexpr int kPassesMax = 6;
@@ -65,6 +66,8 @@ enum : int {
 struct Counters {
   int nact[2];        // active (uninserted) points, by round parity
   int ncand;          // candidates of the current round
+  int nbig;           // searches of the round deferred to k_cavity_big
+  int nbigw;          // stars of the pass deferred to k_commit_big
   int pool_used;      // ints of the cavity pool used in the current round
   int nsimp;          // simplex slots handed out (high-water mark)
   int wasted;         // slots reserved by allocations that did not fit
@@ -138,6 +141,8 @@ struct DevTree {
   int4* cinfo;    // (ncav, nfac, pool offset, status)
   int* wl[2];     // work lists (candidate indices), stage s in wl[s & 1]
   int* win;       // winners of the round (adjacent mode)
+  int* bigc;      // candidates whose search k_cavity_big finishes (nbig of them)
+  int* bigw;      // winners whose star k_commit_big writes (nbigw of them)
   int* repl;      // per (slot << 2 | face): new simplex code on that face (adjacent mode)
   int* pool;
   int2* dups;     // (dropped vid, vid it equals)
@@ -244,6 +249,7 @@ struct Tuning {
   int thin;
   int adjacent;  // 1: cavities of one pass may touch (see k_check in vd_build.cu)
   int exact_int;  // 1: conflict tests use the integer exact tier before the expansions
+  int big_block;  // 1: oversized searches and stars go to whole-block kernels (k_cavity_big, k_commit_big)
 };
 // Kernel types for profiling.
 enum {
@@ -258,13 +264,15 @@ enum {
   KT_DECIDE,
   KT_FIX,
   KT_SMALL,
+  KT_BIG,
+  KT_BIGW,
   KT_COUNT
 };
 extern const char* const kKernelTypeNames[KT_COUNT];
 // Event log of one round: ev[0] before the first kernel, ev[i + 1] after
 // kernel i, whose type is type[i].
 struct Prof {
-  static constexpr int kMax = 5 + 3 * kPassesMax;
+  static constexpr int kMax = 6 + 4 * kPassesMax;
   cudaEvent_t ev[kMax + 1];
   int type[kMax];
   int n;
