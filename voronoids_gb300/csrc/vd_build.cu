@@ -204,6 +204,8 @@ __global__ void k_upload(DevTree T, const double* xyz, long long n, int base) {
 // the only FP64 work (the FP64 pipe of this GPU is narrow); the cell of a
 // coarser level l is this one shifted right by hint_levels - l, the same
 // cell as floor(u * 2^l) gives directly.
+// Most hint levels of a set (2D single set: 9).
+constexpr int kHintLevelsMax = 9;
 template <int D>
 __device__ __forceinline__ void hint_cell(const SetGeo& g, const vdp::VPt& p, int* ic) {
   const int side = 1 << g.hint_levels;
@@ -382,7 +384,13 @@ __device__ __forceinline__ void activate_body(DevTree T, unsigned long long seed
       cur = -1;
       int ic[3];
       hint_cell<D>(g, p, ic);
-      for (int l = g.hint_levels; l >= 0 && cur < 0; --l) cur = T.hint[hint_at<D>(g, ic, l)];
+      // every level's hint in one round trip, then the finest that is set
+      int hv[kHintLevelsMax + 1];
+#pragma unroll
+      for (int l = 0; l <= kHintLevelsMax; ++l) hv[l] = l <= g.hint_levels ? T.hint[hint_at<D>(g, ic, l)] : -1;
+#pragma unroll
+      for (int l = kHintLevelsMax; l >= 0; --l)
+        if (cur < 0) cur = hv[l];
       if (cur < 0) cur = g.root;  // no insertion into the set yet: its super simplex
       int4 v, nn;
       load_simplex(T, cur, v, nn);

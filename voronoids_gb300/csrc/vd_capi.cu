@@ -443,7 +443,10 @@ void release(vd_tree* t) {
 // Finest location-hint level of a single-set tree (its size is not known
 // when it is created) and of a set of n points in a batched build (about two
 // points per finest cell).
-int single_hint_levels(int dim) { return dim == 3 ? 6 : 9; }
+#ifndef VD_HINT_LEVELS_3D
+#define VD_HINT_LEVELS_3D 5
+#endif
+int single_hint_levels(int dim) { return dim == 3 ? VD_HINT_LEVELS_3D : 9; }
 int set_hint_levels(int dim, int64_t n) {
   int l = 0;
   const int per = dim == 3 ? 8 : 4;
