@@ -662,29 +662,50 @@ __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl,
 // Thinning test of one nominee (one thread): it must hold the thinning claim
 // on its simplex and on every face neighbour; with `thin` >= 2 no lower
 // nominee may claim a simplex two faces away either.
+// Exact coordinate equality (as vdp::same_point) on the bit patterns, with
+// +0 and -0 equal: integer compares instead of FP64 ones.
+__device__ __forceinline__ bool same_bits(double a, double b) {
+  const unsigned long long x = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long y = (unsigned long long)__double_as_longlong(b);
+  return x == y || ((x | y) << 1) == 0ull;
+}
+__device__ __forceinline__ bool same_point_bits(const vdp::VPt& a, const vdp::VPt& b) {
+  return same_bits(a.x, b.x) && same_bits(a.y, b.y) && same_bits(a.z, b.z);
+}
+
 template <int D>
 __device__ bool thin_lost1(const DevTree& T, int home, int4 n0, unsigned long long key, int thin) {
   constexpr int NV = D + 1;
   if (thin == 0) return false;
-  if (T.thin[home] != key) return true;
+  // every load is issued before any test decides, so that the claims of the
+  // home simplex, its face neighbours and (thin >= 2) their neighbours
+  // arrive in two round trips
+  int nb[NV];
   for (int f = 0; f < NV; ++f) {
-    const int nb = get4(n0, f);
-    if (nb < 0 || bad_simp(T, nb >> 2)) continue;
-    if (T.thin[nb >> 2] != key) return true;
+    const int x = get4(n0, f);
+    nb[f] = (x < 0 || bad_simp(T, x >> 2)) ? -1 : x >> 2;
   }
-  if (thin >= 2) {
-    for (int f = 0; f < NV; ++f) {
-      const int nb = get4(n0, f);
-      if (nb < 0 || bad_simp(T, nb >> 2)) continue;
-      int4 v2, n2;
-      load_simplex(T, nb >> 2, v2, n2);
-      for (int g = 0; g < NV; ++g) {
-        const int x = get4(n2, g);
-        if (x >= 0 && !bad_simp(T, x >> 2) && T.thin[x >> 2] < key) return true;
-      }
+  unsigned long long th[NV];
+  int4 n2[NV];
+  const unsigned long long own = T.thin[home];
+  for (int f = 0; f < NV; ++f) {
+    th[f] = nb[f] >= 0 ? T.thin[nb[f]] : key;
+    n2[f] = make_int4(-1, -1, -1, -1);
+    if (thin >= 2 && nb[f] >= 0) {
+      int4 v2;
+      load_simplex(T, nb[f], v2, n2[f]);
     }
   }
-  return false;
+  bool lost = own != key;
+  for (int f = 0; f < NV; ++f) lost |= th[f] != key;
+  if (thin >= 2) {
+    for (int f = 0; f < NV; ++f)
+      for (int g = 0; g < NV; ++g) {
+        const int x = get4(n2[f], g);
+        if (x >= 0 && !bad_simp(T, x >> 2)) lost |= T.thin[x >> 2] < key;
+      }
+  }
+  return lost;
 }
 
 // Per nominee (one thread): duplicate test against the vertices of its
@@ -707,7 +728,7 @@ __device__ __forceinline__ void thin_body(DevTree T, int thin, int bid, int nblk
       int dup = -1;
       for (int j = 0; j < NV; ++j) {
         const int vid = get4(v, j);
-        if (vdp::same_point(load_pt(T, vid), q)) dup = vid;
+        if (same_point_bits(load_pt(T, vid), q)) dup = vid;
       }
       if (dup >= 0) {
         T.act[par][e.w].x = -1;
