@@ -1537,14 +1537,15 @@ __device__ __forceinline__ void reclaim_body(DevTree T, int pass, int adjacent, 
     int *P, *F, ncav, nfac;
     bool big;
     cand_lists(T, info, P, F, ncav, nfac, big);
+    // bitwise ors: every mark is loaded, none waits for an earlier verdict
     bool blocked = false;
     for (int i = lane; i < ncav; i += 32) {
       const int s = P[i];
-      blocked = blocked || T.killed[s].x == round || T.touched[s] == round;
+      blocked |= (T.killed[s].x == round) | (T.touched[s] == round);
     }
     for (int j = lane; j < nfac; j += 32) {
       const int o = F[6 * j + 4];
-      if (o >= 0) blocked = blocked || T.killed[o >> 2].x == round;
+      if (o >= 0) blocked |= T.killed[o >> 2].x == round;
     }
     if (__any_sync(FULL, blocked)) {
       if (lane == 0) T.cinfo[c].w = ST_LOST;
