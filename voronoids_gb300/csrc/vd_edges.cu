@@ -150,6 +150,37 @@ __global__ void __launch_bounds__(256) k_edge_uniq(int n_in, const int* off, int
       if (lane == 0) ucnt[u] = L;
       continue;
     }
+    if (L <= 64) {
+      // common case: two keys per lane (positions lane, lane + 32), bitonic
+      // network on registers and shuffles, no shared memory
+      int a = lane < L ? buf[b + lane] : 0x7fffffff;
+      int c = lane + 32 < L ? buf[b + lane + 32] : 0x7fffffff;
+      for (int k = 2; k <= 64; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+          if (j == 32) {  // k == 64: pairs (lane, lane + 32), ascending
+            const int lo = min(a, c), hi = max(a, c);
+            a = lo;
+            c = hi;
+            continue;
+          }
+          const bool lower = (lane & j) == 0;
+          const int ya = __shfl_xor_sync(FULL, a, j), yc = __shfl_xor_sync(FULL, c, j);
+          const bool upa = (lane & k) == 0, upc = ((lane + 32) & k) == 0;
+          a = (lower == upa) ? min(a, ya) : max(a, ya);
+          c = (lower == upc) ? min(c, yc) : max(c, yc);
+        }
+      // unique: keep the first of each run
+      const int pa = __shfl_up_sync(FULL, a, 1), pc = __shfl_up_sync(FULL, c, 1);
+      const int a31 = __shfl_sync(FULL, a, 31);
+      const bool ka = lane < L && (lane == 0 || a != pa);
+      const bool kc = lane + 32 < L && c != (lane == 0 ? a31 : pc);
+      const unsigned ma = __ballot_sync(FULL, ka), mc = __ballot_sync(FULL, kc);
+      const unsigned below = (1u << lane) - 1;
+      if (ka) buf[b + __popc(ma & below)] = a;
+      if (kc) buf[b + __popc(ma) + __popc(mc & below)] = c;
+      if (lane == 0) ucnt[u] = __popc(ma) + __popc(mc);
+      continue;
+    }
     int P = 2;
     while (P < L) P <<= 1;
     for (int i = lane; i < P; i += 32) a[i] = i < L ? buf[b + i] : 0x7fffffff;
