@@ -200,19 +200,19 @@ __global__ void k_upload(DevTree T, const double* xyz, long long n, int base) {
 // races are harmless: any live simplex of the set is a valid walk start, a
 // near one is a short walk).
 //
-// Cell of p at the finest level of set g, per axis.  The coordinate map is
-// the only FP64 work (the FP64 pipe of this GPU is narrow); the cell of a
-// coarser level l is this one shifted right by hint_levels - l, the same
-// cell as floor(u * 2^l) gives directly.
+// Cell of p at the finest level of set g, per axis, from the f32 high parts
+// of its split coordinates (a hint cell need not be exact, and the FP64 pipe
+// of this GPU is narrow); the cell of a coarser level l is this one shifted
+// right by hint_levels - l, the same cell as floor(u * 2^l) gives directly.
 // Most hint levels of a set (2D single set: 9).
 constexpr int kHintLevelsMax = 9;
 template <int D>
-__device__ __forceinline__ void hint_cell(const SetGeo& g, const vdp::VPt& p, int* ic) {
+__device__ __forceinline__ void hint_cell(const SetGeo& g, const vdp::FPt& p, int* ic) {
   const int side = 1 << g.hint_levels;
-  const double c[3] = {p.x, p.y, p.z};
+  const float c[3] = {p.hx, p.hy, p.hz};
   for (int k = 0; k < D; ++k) {
-    const double u = (c[k] - g.org[k]) * g.scale;
-    int i = u > 0.0 ? (int)fmin(u * side, (double)side) : 0;
+    const float u = (c[k] - g.orgf[k]) * g.scalef;
+    const int i = u > 0.0f ? (int)fminf(u * (float)side, (float)side) : 0;
     ic[k] = i >= side ? side - 1 : i;
   }
 }
@@ -226,7 +226,7 @@ __device__ __forceinline__ int hint_at(const SetGeo& g, const int* ic, int level
 }
 
 template <int D>
-__device__ __forceinline__ void write_hints(const DevTree& T, int vid, const vdp::VPt& q, int slot) {
+__device__ __forceinline__ void write_hints(const DevTree& T, int vid, const vdp::FPt& q, int slot) {
   const SetGeo& g = T.sets[set_index(T, vid)];
   int ic[3];
   hint_cell<D>(g, q, ic);
@@ -379,11 +379,11 @@ __device__ __forceinline__ void activate_body(DevTree T, unsigned long long seed
         vid = 0;
       }
       pr = priority((uint32_t)vid, seed);
-      const vdp::VPt p = load_pt(T, vid);
+      const vdp::FPt fp = load_fpt(T, vid);
       const SetGeo& g = T.sets[set_index(T, vid)];
       cur = -1;
       int ic[3];
-      hint_cell<D>(g, p, ic);
+      hint_cell<D>(g, fp, ic);
       // every level's hint in one round trip, then the finest that is set
       int hv[kHintLevelsMax + 1];
 #pragma unroll
@@ -402,14 +402,13 @@ __device__ __forceinline__ void activate_body(DevTree T, unsigned long long seed
         }
         load_simplex(T, cur, v, nn);
       }
-      const vdp::FPt fp = load_fpt(T, vid);
       int step = 0;
       for (; step < cap; ++step) {
         vdp::FPt fv[NV];
         for (int j = 0; j < NV; ++j) fv[j] = load_fpt(T, get4(v, j));
         auto load64 = [&](vdp::VPt* v64, vdp::VPt& p64) {
           for (int j = 0; j < NV; ++j) v64[j] = load_pt(T, get4(v, j));
-          p64 = p;
+          p64 = load_pt(T, vid);  // the f64 point only on the fallback path
         };
         const int f = vdp::exit_face_hl<D>(fv, fp, (1u << NV) - 1, tl, perr, load64);
         if (f < 0) break;
@@ -1413,7 +1412,7 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
         publish_shared_facets<false>(T, F, P, IDS, nfac, round, lane);
       }
       if (lane == 0) {
-        write_hints<D>(T, cd.x, load_pt(T, cd.x), id0);
+        write_hints<D>(T, cd.x, load_fpt(T, cd.x), id0);
         T.cinfo[c].w = ST_DONE;
         T.act[par][cd.w].x = -1;
       }
@@ -1472,7 +1471,7 @@ __global__ void __launch_bounds__(512, 1) k_commit_big(DevTree T) {
     write_star_big<D, true>(T, F, ID, nfac, round, P + kOffR, threadIdx.x);
     publish_shared_facets<true>(T, F, P, ID, nfac, round, threadIdx.x);
     if (threadIdx.x == 0) {
-      write_hints<D>(T, cd.x, load_pt(T, cd.x), id0);
+      write_hints<D>(T, cd.x, load_fpt(T, cd.x), id0);
       T.cinfo[c].w = ST_DONE;
       T.act[par][cd.w].x = -1;
     }

@@ -581,6 +581,8 @@ int set_geometry_sets(vd_tree* t, int nsets, const double* c, const double* rb, 
     vd::SetGeo& g = geo[s];
     for (int k = 0; k < 3; ++k) g.org[k] = (k < dim ? c[3 * s + k] : 0.0) - rb[s];
     g.scale = rb[s] > 0 ? 1.0 / (2.0 * rb[s]) : 1.0;
+    for (int k = 0; k < 3; ++k) g.orgf[k] = (float)g.org[k];
+    g.scalef = (float)g.scale;
     g.hint_levels = sizes ? set_hint_levels(dim, sizes[s]) : single_hint_levels(dim);
     g.hint_off = (int)cells;
     g.root = s;

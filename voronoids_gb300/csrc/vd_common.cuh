@@ -119,6 +119,8 @@ struct alignas(16) SetGeo {
   int root;         // slot of the set's super simplex
   int n;            // input points of the set (batched build)
   int sup[4];       // super-simplex vertex ids, positively oriented (-1 pads 2D)
+  float orgf[3];    // org and scale rounded to f32: hint cells are mapped in FP32
+  float scalef;
 };
 
 // Hint cells of levels 0..levels.
