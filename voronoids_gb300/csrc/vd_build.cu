@@ -434,12 +434,19 @@ template <int D>
 __global__ void VD_WALK_BOUNDS k_activate(DevTree T, unsigned long long seed) { activate_body<D>(T, seed, blockIdx.x, gridDim.x); }
 
 // ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ bool screen_nominee(const DevTree& T, int c, int4 e, int thin, int round);
+
+// With thin == 0 the nominees are screened here (duplicates only; k_thin is
+// not launched): the survivors go straight to work list stage 0, whose count
+// k_relocate of the previous round set to 0.
+template <int D>
 __device__ __forceinline__ void pick_body(DevTree T, int thin, int bid, int nblk) {
   const int round = T.ctr->round;
   const int par = round & 1;
   if (bid == 0 && threadIdx.x == 0) {
     T.ctr->nact[par ^ 1] = 0;
-    for (int k = 0; k < kStages; ++k) T.ctr->nwl[k] = 0;
+    for (int k = 1; k < kStages; ++k) T.ctr->nwl[k] = 0;
     T.ctr->nwin = 0;
     T.ctr->win_lo = 0;
   }
@@ -455,6 +462,11 @@ __device__ __forceinline__ void pick_body(DevTree T, int thin, int bid, int nblk
       is = e.x >= 0 && T.vote[e.y] == (ep | (unsigned)e.z);
     }
     int k = warp_append(&T.ctr->ncand, is);
+    if (thin == 0) {
+      const bool surv = is && k < T.cap_cand && screen_nominee<D>(T, k, make_int4(e.x, e.y, e.z, i), 0, round);
+      const int w = warp_append(&T.ctr->nwl[0], surv);
+      if (surv) T.wl[0][w] = k;
+    }
     if (is) {
       ++ncand;
       if (k < T.cap_cand) T.cand[k] = make_int4(e.x, e.y, e.z, i);
@@ -472,7 +484,8 @@ __device__ __forceinline__ void pick_body(DevTree T, int thin, int bid, int nblk
   ncand = warp_sum(ncand);
   if ((threadIdx.x & 31) == 0 && ncand) atomicAdd(&T.ctr->candidates, ncand);
 }
-__global__ void k_pick(DevTree T, int thin) { pick_body(T, thin, blockIdx.x, gridDim.x); }
+template <int D>
+__global__ void k_pick(DevTree T, int thin) { pick_body<D>(T, thin, blockIdx.x, gridDim.x); }
 
 // Headers of a warp's items in a grid-stride loop over a candidate list,
 // staged in shared memory: lane k loads item it0 + k * nw (its candidate,
@@ -707,39 +720,43 @@ __device__ bool thin_lost1(const DevTree& T, int home, int4 n0, unsigned long lo
   return lost;
 }
 
+// One nominee c (record e): duplicate test against the vertices of its
+// simplex, then the thinning test.  Returns whether it goes on to the search.
+template <int D>
+__device__ __forceinline__ bool screen_nominee(const DevTree& T, int c, int4 e, int thin, int round) {
+  constexpr int NV = D + 1;
+  const int par = round & 1;
+  int4 v, n;
+  load_simplex(T, e.y, v, n);
+  const vdp::VPt q = load_pt(T, e.x);
+  int dup = -1;
+  for (int j = 0; j < NV; ++j) {
+    const int vid = get4(v, j);
+    if (same_point_bits(load_pt(T, vid), q)) dup = vid;
+  }
+  if (dup >= 0) {
+    T.act[par][e.w].x = -1;
+    const int k = atomicAdd(&T.ctr->ndup, 1);
+    if (k < T.cap_dups) T.dups[k] = make_int2(e.x, dup);
+    T.cinfo[c] = make_int4(0, 0, 0, ST_DUP);
+    return false;
+  }
+  if (thin_lost1<D>(T, e.y, n, epoch(round) | (unsigned)e.z, thin)) {
+    T.cinfo[c] = make_int4(0, 0, 0, ST_LOST);
+    return false;
+  }
+  return true;
+}
+
 // Per nominee (one thread): duplicate test against the vertices of its
 // simplex and the thinning test; survivors go to work list stage 0.
 template <int D>
 __device__ __forceinline__ void thin_body(DevTree T, int thin, int bid, int nblk) {
   const int round = T.ctr->round;
-  constexpr int NV = D + 1;
   const int nc = min(T.ctr->ncand, T.cap_cand);
-  const unsigned long long ep = epoch(round);
-  const int par = round & 1;
   for (int b = bid * blockDim.x; b < nc; b += nblk * blockDim.x) {
     const int c = b + threadIdx.x;
-    bool survive = false;
-    if (c < nc) {
-      const int4 e = T.cand[c];
-      int4 v, n;
-      load_simplex(T, e.y, v, n);
-      const vdp::VPt q = load_pt(T, e.x);
-      int dup = -1;
-      for (int j = 0; j < NV; ++j) {
-        const int vid = get4(v, j);
-        if (same_point_bits(load_pt(T, vid), q)) dup = vid;
-      }
-      if (dup >= 0) {
-        T.act[par][e.w].x = -1;
-        const int k = atomicAdd(&T.ctr->ndup, 1);
-        if (k < T.cap_dups) T.dups[k] = make_int2(e.x, dup);
-        T.cinfo[c] = make_int4(0, 0, 0, ST_DUP);
-      } else if (thin_lost1<D>(T, e.y, n, ep | (unsigned)e.z, thin)) {
-        T.cinfo[c] = make_int4(0, 0, 0, ST_LOST);
-      } else {
-        survive = true;
-      }
-    }
+    const bool survive = c < nc && screen_nominee<D>(T, c, T.cand[c], thin, round);
     const int k = warp_append(&T.ctr->nwl[0], survive);
     if (survive) T.wl[0][k] = c;
   }
@@ -1570,6 +1587,7 @@ __device__ __forceinline__ void relocate_body(DevTree T, int bid, int nblk) {
   const int par = round & 1;
   if (bid == 0 && threadIdx.x == 0) {
     T.ctr->ncand = 0;
+    T.ctr->nwl[0] = 0;  // k_pick may append to stage 0 (thin == 0)
     T.ctr->pool_used = 0;
     T.ctr->nbig = 0;
   }
@@ -1688,10 +1706,12 @@ __global__ void __launch_bounds__(128) k_rounds_small(DevTree T, Tuning tu, unsi
     if (!grid_sync(c, nblk)) return;
     activate_body<D>(T, seed, bid, nblk);
     if (!grid_sync(c, nblk)) return;
-    pick_body(T, tu.thin, bid, nblk);
+    pick_body<D>(T, tu.thin, bid, nblk);
     if (!grid_sync(c, nblk)) return;
-    thin_body<D>(T, tu.thin, bid, nblk);
-    if (!grid_sync(c, nblk)) return;
+    if (tu.thin > 0) {
+      thin_body<D>(T, tu.thin, bid, nblk);
+      if (!grid_sync(c, nblk)) return;
+    }
     cavity_body<D, 0>(T, tu.adjacent, bid, nblk, reinterpret_cast<WarpCav<D>*>(dsm), false);
     if (!grid_sync(c, nblk)) return;
     for (int p = 0; p < tu.passes; ++p) {
@@ -1746,15 +1766,17 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
     }
   };
   if (pf && pf->n == 0) cudaEventRecord(pf->ev[0], L.stream);
-  note_launches((tu.adjacent ? 6 + 3 * tu.passes - 1 : 6 + 2 * tu.passes - 1) +
+  note_launches((tu.adjacent ? 6 + 3 * tu.passes - 1 : 6 + 2 * tu.passes - 1) - (tu.thin > 0 ? 0 : 1) +
                 (tu.big_block ? 1 + (tu.adjacent ? tu.passes : 0) : 0));
   k_plan<<<1, 32, 0, L.stream>>>(T, fd.ratio);
   k_activate<D><<<L.blocks, 256, 0, L.stream>>>(T, fd.seed);
   mark(KT_ACTIVATE);
-  k_pick<<<L.blocks, 256, 0, L.stream>>>(T, tu.thin);
+  k_pick<D><<<L.blocks, 256, 0, L.stream>>>(T, tu.thin);
   mark(KT_PICK);
-  k_thin<D><<<L.blocks, 256, 0, L.stream>>>(T, tu.thin);
-  mark(KT_THIN);
+  if (tu.thin > 0) {
+    k_thin<D><<<L.blocks, 256, 0, L.stream>>>(T, tu.thin);
+    mark(KT_THIN);
+  }
   // kernels with conflict tests come in two forms: exact tier on expansions
   // alone (small register allocation) or integer tier first (tu.exact_int)
   if (tu.exact_int)
