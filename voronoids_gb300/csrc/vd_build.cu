@@ -1074,11 +1074,9 @@ __device__ void write_star(const DevTree& T, WarpCommit<D>& W, const int* __rest
     emit_simplex(T, r, W.id[j], set4(make_int4(-1, -1, -1, -1), qf, r[4]), round);
   }
   const int sweeps = (nfac * D / 2 + PER_SWEEP - 1) / PER_SWEEP;
+  // the table is empty on entry (cleared when the warp starts, and after
+  // every sweep by the check below)
   for (int sw = 0; sw < sweeps; ++sw) {
-    for (int i = lane; i < HR; i += 32) {
-      W.rk[i] = EMPTY;
-      W.ra[i] = -1;
-    }
     __syncwarp();  // also orders the record stores above before the link stores below
     for (int j = lane; j < nfac; j += 32) {
       // the facet record in three 8-byte loads (records are 8-byte aligned)
@@ -1113,9 +1111,13 @@ __device__ void write_star(const DevTree& T, WarpCommit<D>& W, const int* __rest
       }
     }
     __syncwarp();
-    // a ridge with one half would be a broken star
-    for (int i = lane; i < HR; i += 32)
+    // a ridge with one half would be a broken star; the table is emptied
+    // for the next sweep or star
+    for (int i = lane; i < HR; i += 32) {
       if (W.ra[i] >= 0) set_error(T.ctr, E_INTERNAL);
+      W.rk[i] = EMPTY;
+      W.ra[i] = -1;
+    }
     __syncwarp();
   }
 }
@@ -1249,6 +1251,14 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
   // MODE 1 gets only the item headers in shared memory, the others a WarpCommit each
   WarpCommit<D>& W = reinterpret_cast<WarpCommit<D>*>(dsm)[wib];
   HeadBuf& H = MODE == 1 ? reinterpret_cast<HeadBuf*>(dsm)[wib] : W.hb;
+  if (MODE != 1) {
+    // empty ridge table for write_star (which leaves it empty after each star)
+    for (int i = lane; i < WarpCommit<D>::HR; i += 32) {
+      W.rk[i] = ~0ull;
+      W.ra[i] = -1;
+    }
+    __syncwarp();
+  }
   const unsigned long long pe = pass_epoch(round, pass);
   const int par = round & 1;
   unsigned long long nwon = 0, ncreated = 0, nkilled = 0;
