@@ -3,25 +3,36 @@
 // One round replaces one `add_points_to_tree` batch of the reference
 // (src/delaunay_tree.rs:336-386; queue + placement in src/scheduler.rs:6-55):
 //
+//   k_plan      one thread opens the round and activates priority levels.
+//   k_activate  newly fed points walk from a location hint to the simplex
+//               that contains them and vote.
 //   k_pick      every simplex that holds uninserted points nominates the one
-//               with the lowest priority (votes were cast by the previous
-//               k_relocate); a nominee claims its simplex and the face
-//               neighbours (thinning) so that only locally lowest nominees
-//               pay for a cavity search.
-//   k_cavity    one warp per surviving nominee: breadth-first search of the
-//               conflict region from the simplex that contains it (`locate` +
+//               with the lowest priority (votes were cast by k_activate and
+//               the previous k_relocate); a nominee claims its simplex and
+//               the face neighbours (thinning) so that only locally lowest
+//               nominees pay for a cavity search.
+//   k_thin      nominees that lose a thinning claim, or duplicate a vertex of
+//               their simplex, drop out (with thinning radius 0, k_pick does
+//               the duplicate test and this kernel is not launched).
+//   k_cavity    one warp per surviving nominee: search of the conflict region
+//               from the simplex that contains it (`locate` +
 //               `find_all_neighbors`, src/delaunay_tree.rs:33-75) with exact
 //               perturbed in-sphere tests, collection of the boundary facets
 //               (`get_new_simplices`, :77-123), then atomicMin claims with the
-//               candidate's priority on the cavity (claim_c) and on every outer
-//               neighbour whose face it will rewrite (claim_n).
+//               candidate's priority on the cavity (claim_c) and, in the
+//               strict round mode, on every outer neighbour (claim_n).
+//               Regions that outgrow a warp's shared memory are searched
+//               again in the pool (by the warp, or by a block of
+//               k_cavity_big once a call has had one).
 //   k_check /   resolution passes, one warp per candidate: the independence
 //   k_reclaim   test (see k_check), then winners write the star (killed slots
 //               first, then fresh slots), link it internally by matching ridges
 //               (`pair_simplices`, :674-695) and repoint the outer faces
-//               (`insert_points_parallel`, :213-334).  Winners are pairwise
-//               independent: no winner's point lies in another winner's new
-//               simplices, so a round equals some sequential insertion order.
+//               (`insert_points_parallel`, :213-334).  In the default adjacent
+//               mode a decide half and a commit half are separate kernels, and
+//               the stars of winners that share a facet are stitched at the
+//               start of k_relocate.  A round equals some sequential insertion
+//               order.
 //   k_relocate  one thread per uninserted point: points whose simplex was
 //               removed walk inside the new star (faces through the new vertex
 //               only) to the simplex that contains them; every point then votes
@@ -30,7 +41,7 @@
 // A point is always located in a simplex that contains it, and a closed
 // simplex meets its circumsphere only in its vertices, so the containing
 // simplex is in conflict unless the point duplicates one of its vertices,
-// which k_cavity detects and drops.
+// which k_thin (or k_pick) detects and drops.
 #include <cuda_runtime.h>
 
 #include <algorithm>
