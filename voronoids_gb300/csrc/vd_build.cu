@@ -1821,7 +1821,8 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
   for (int p = 0; p < tu.passes; ++p) {
     const int last = p == tu.passes - 1;
     if (p > 0) {
-      k_reclaim<D><<<L.warps / 4, 128, 0, L.stream>>>(T, p, tu.adjacent);
+      // reclaim (40 registers, no shared memory) runs twice the search's warps
+      k_reclaim<D><<<L.warps / 2, 128, 0, L.stream>>>(T, p, tu.adjacent);
       mark(KT_RECLAIM);
     }
     if (tu.adjacent) {
