@@ -1955,9 +1955,8 @@ void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, 
     round_impl<2>(T, L, tu, fd, pf);
 }
 
-const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_thin",     "k_cavity", "k_check",
-                                                "k_reclaim",  "k_relocate", "k_activate", "edges",
-                                                "k_decide",   "k_fix_links", "k_rounds_small", "k_cavity_big",
-                                                "k_commit_big"};
+const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_thin",         "k_cavity",     "k_check",
+                                                "k_reclaim",  "k_relocate",     "k_activate",   "edges",
+                                                "k_decide",   "k_rounds_small", "k_cavity_big", "k_commit_big"};
 
 }  // namespace vd

@@ -264,7 +264,6 @@ enum {
   KT_ACTIVATE,
   KT_EDGES,
   KT_DECIDE,
-  KT_FIX,
   KT_SMALL,
   KT_BIG,
   KT_BIGW,
