@@ -68,3 +68,27 @@ def test_bad_arguments_are_rejected_on_host():
     r = ctypes.c_double()
     assert L.vd_super_simplex(2, q.ctypes.data_as(dp), 1, out.ctypes.data_as(dp), ctypes.byref(r)) == 5
     assert L.vd_insert_points(None, p.ctypes.data_as(dp), 3, 0) == 1
+
+
+def test_profile_kernel_names():
+    """The per-kernel profile slots have unique names, the round's kernels
+    among them, and the roofline kernels' committed ncu summaries carry a
+    traffic figure the bench can read."""
+    import bench
+    from voronoids_gb300 import _native
+    L = _native.load()
+    names = []
+    i = 0
+    while True:
+        nm = L.vd_profile_name(i)
+        if not nm:
+            break
+        names.append(nm.decode())
+        i += 1
+    assert len(names) == len(set(names))
+    for k in ("k_pick", "k_thin", "k_cavity", "k_check", "k_reclaim", "k_relocate", "k_activate", "k_decide",
+              "k_cavity_big", "k_commit_big", "edges"):
+        assert k in names
+    for k in ("k_cavity", "k_check", "k_decide"):
+        t = bench.profile_traffic(k)
+        assert t is not None and t > 1e6
