@@ -125,7 +125,7 @@ int vd_num_vertices(vd_tree* t, int64_t* n);
  * simplex created, counting the reference's initial 5 (3D) / 4 (2D). */
 int vd_max_simplex_id(vd_tree* t, int64_t* id);
 
-/* Live simplices, as the reference's simplex map (src/lib.rs:142-156):
+/* Live simplices, as the reference's simplex map (src/lib.rs:87-100):
  * verts[4*i + j] = vertex j of simplex i (super vertices are -(1+k), k = 0..dim;
  * in 2D verts[4*i+3] = -1); nbrs[4*i + j] = simplex across the face opposite
  * vertex j, or -1 on the hull.  *n receives the count. */
@@ -153,6 +153,24 @@ int vd_edges_u32(vd_tree* t, uint32_t* uv, int64_t cap, int64_t* n);
  * (NULL or 6 entries): non-positive, asymmetric, not Delaunay, not
  * perturbed-Delaunay, hull facets, facets checked. */
 int vd_check_delaunay(vd_tree* t, int* ok, int64_t* violations);
+
+/* check_delaunay (src/delaunay_tree.rs:512-541, :642-671) on a caller's
+ * triangulation rather than a tree's: the same exact device checks as
+ * vd_check_delaunay, for simplices built anywhere (an exported and edited
+ * tree, another library's output).
+ *   pts      host, npts rows of `dim` doubles; vertex id i is row i (the
+ *            caller includes any super vertices)
+ *   verts    host, ns rows of 4 int32 vertex ids, positively oriented as
+ *            vd_simplices exports them (2D: the 4th id is ignored)
+ *   nbrs     host, ns rows of 4 int32: the simplex across the face opposite
+ *            vertex j, or -1 on the hull
+ * *ok = 1 iff no simplex is non-positive, no link is one-sided or out of
+ * range, and every interior facet is locally Delaunay (exact and perturbed by
+ * vertex id).  `violations` (NULL or 6 entries) as vd_check_delaunay; a vertex
+ * id outside [0, npts) counts as a structural (asymmetric) fault.  Allocates
+ * and frees its own device buffers; synchronous. */
+int vd_check_triangulation(int dim, const double* pts, int64_t npts, const int32_t* verts, const int32_t* nbrs,
+                           int64_t ns, int* ok, int64_t* violations);
 
 /* Duplicates skipped so far: pairs (skipped vertex, vertex it equals). */
 int vd_duplicates(vd_tree* t, int64_t* pairs, int64_t cap, int64_t* n);
@@ -316,12 +334,14 @@ void vd_server_free(vd_server* s);
  *           rejected with VD_ERR_ARG
  *   d_uv    device output, (u, v) uint32 pairs, u < v, sorted; *n_edges gets
  *           the count (VD_ERR_ARG if it exceeds cap)
- *   stream  cudaStream_t (NULL = default stream); the call returns after its
- *           work on that stream has finished.
+ *   stream  cudaStream_t (NULL = default stream); the call is synchronous:
+ *           it returns after its work on that stream has finished.
  * All calls on a device share the scratch array and leave their data in it;
  * calls whose GPU work overlaps race and give wrong results.  The first call
  * on a device looks up the array's address (cudaGetSymbolAddress) with that
- * device current; make it before starting any stream capture. */
+ * device current, and looks it up again once the device's context has been
+ * recreated (e.g. after cudaDeviceReset); make that first call before starting
+ * any stream capture. */
 int vd_edges_from_simplices_noalloc(int dim, const int32_t* d_simp, int64_t ns, int64_t nverts,
                                     uint32_t* d_uv, int64_t cap, int64_t* n_edges, void* stream);
 

@@ -304,6 +304,46 @@ int orient(int dim, const P3* p, long long* nexact) {
   return exact_orient(dim, p);
 }
 
+// Sign of the unperturbed lifted determinant from an f64 evaluation with a
+// permanent-based error bound; 0 when the bound cannot decide (the caller
+// then evaluates it exactly).
+int lifted_filter(int dim, const P3* p, const P3& q) {
+  const int nv = dim + 1;
+  double x[4], y[4], z[4], mx = 0;
+  for (int i = 0; i < nv; ++i) {
+    x[i] = p[i].x - q.x;
+    y[i] = p[i].y - q.y;
+    z[i] = p[i].z - q.z;
+    mx = std::max({mx, std::fabs(x[i]), std::fabs(y[i]), std::fabs(z[i])});
+  }
+  if (!(mx < 1e30)) return 0;
+  double det = 0, perm = 0;
+  for (int i = 0; i < nv; ++i) {
+    int o[3], t = 0;
+    for (int k = 0; k < nv; ++k)
+      if (k != i) o[t++] = k;
+    double Oi, Pi;
+    if (dim == 3) {
+      auto m = [&](int a, int b) { return x[a] * y[b] - y[a] * x[b]; };
+      auto pm = [&](int a, int b) { return std::fabs(x[a] * y[b]) + std::fabs(y[a] * x[b]); };
+      Oi = z[o[0]] * m(o[1], o[2]) - z[o[1]] * m(o[0], o[2]) + z[o[2]] * m(o[0], o[1]);
+      Pi = std::fabs(z[o[0]]) * pm(o[1], o[2]) + std::fabs(z[o[1]]) * pm(o[0], o[2]) +
+           std::fabs(z[o[2]]) * pm(o[0], o[1]);
+      if (!(i & 1)) Oi = -Oi;
+    } else {
+      Oi = x[o[0]] * y[o[1]] - y[o[0]] * x[o[1]];
+      Pi = std::fabs(x[o[0]] * y[o[1]]) + std::fabs(y[o[0]] * x[o[1]]);
+      if (i & 1) Oi = -Oi;
+    }
+    const double w = x[i] * x[i] + y[i] * y[i] + z[i] * z[i];
+    det += w * Oi;
+    perm += w * Pi;
+  }
+  if (!(perm > 1e-150)) return 0;
+  const double bound = 64.0 * 1.1102230246251565e-16 * perm;
+  return det > bound ? 1 : (det < -bound ? -1 : 0);
+}
+
 // Perturbed conflict test: +1 inside, -1 outside (never 0).
 int insphere_sos(int dim, const P3* p, const int* key, const P3& q, int qkey, long long* nexact,
                  long long* nsos) {
@@ -1310,60 +1350,74 @@ void vdo_vertices(void* h, double* xyz) {
 void vdo_validate(int dim, const double* verts, int64_t nvert, const int32_t* simp,
                   const int32_t* nbr, int64_t ns, int64_t expect_vertices, long long* out) {
   for (int i = 0; i < 8; ++i) out[i] = 0;
-  int nv = dim + 1;
+  const int nv = dim + 1;
   auto P = [&](int v) { return P3{verts[3 * v], verts[3 * v + 1], verts[3 * v + 2]}; };
-  std::vector<char> seen(nvert, 0);
-  long long nex = 0;
-  for (int64_t s = 0; s < ns; ++s) {
-    const int32_t* v = simp + 4 * s;
-    P3 q[4];
-    for (int i = 0; i < nv; ++i) {
-      q[i] = P(v[i]);
-      seen[v[i]] = 1;
-    }
-    if (orient(dim, q, &nex) <= 0) out[0]++;
-    for (int f = 0; f < nv; ++f) {
-      int o = nbr[4 * s + f];
-      if (o < 0) {
-        out[4]++;
-        continue;
-      }
-      // neighbour must point back and share the facet
-      const int32_t* w = simp + 4 * o;
-      int back = -1;
-      for (int g = 0; g < nv; ++g)
-        if (nbr[4 * o + g] == s) back = g;
-      bool ok = back >= 0;
-      if (ok) {
-        for (int i = 0; i < nv; ++i) {
-          if (i == f) continue;
-          bool found = false;
-          for (int g = 0; g < nv; ++g)
-            if (g != back && w[g] == v[i]) found = true;
-          ok = ok && found;
+  // the simplices are split over host threads, each with its own counts
+  const int nth = (int)std::max<unsigned>(1, std::min<unsigned>(64, std::thread::hardware_concurrency()));
+  std::vector<std::array<long long, 8>> part(nth);
+  auto work = [&](int tid) {
+    std::array<long long, 8> c{};
+    const int64_t lo = ns * tid / nth, hi = ns * (tid + 1) / nth;
+    for (int64_t s = lo; s < hi; ++s) {
+      const int32_t* v = simp + 4 * s;
+      P3 q[4];
+      for (int i = 0; i < nv; ++i) q[i] = P(v[i]);
+      if (orient(dim, q, &c[7]) <= 0) c[0]++;
+      for (int f = 0; f < nv; ++f) {
+        int o = nbr[4 * s + f];
+        if (o < 0) {
+          c[4]++;
+          continue;
         }
+        // neighbour must point back and share the facet
+        const int32_t* w = simp + 4 * o;
+        int back = -1;
+        for (int g = 0; g < nv; ++g)
+          if (nbr[4 * o + g] == s) back = g;
+        bool ok = back >= 0;
+        if (ok) {
+          for (int i = 0; i < nv; ++i) {
+            if (i == f) continue;
+            bool found = false;
+            for (int g = 0; g < nv; ++g)
+              if (g != back && w[g] == v[i]) found = true;
+            ok = ok && found;
+          }
+        }
+        if (!ok) {
+          c[1]++;
+          continue;
+        }
+        if (o < s) continue;  // each interior facet once
+        c[5]++;
+        int opp = w[back];
+        P3 e = P(opp);
+        // unperturbed sign: f64 filter, big integers when it cannot decide
+        int ds = lifted_filter(dim, q, e);
+        if (ds == 0) {
+          int os[4];
+          exact_lifted(dim, q, e, os, &ds);
+          ++c[7];
+        }
+        if (ds > 0) c[2]++;
+        int key[4];
+        for (int i = 0; i < nv; ++i) key[i] = v[i];
+        if (insphere_sos(dim, q, key, e, opp, &c[7], nullptr) > 0) c[3]++;
       }
-      if (!ok) {
-        out[1]++;
-        continue;
-      }
-      if (o < s) continue;  // each interior facet once
-      out[5]++;
-      int opp = w[back];
-      P3 e = P(opp);
-      int ds;
-      int os[4];
-      exact_lifted(dim, q, e, os, &ds);
-      ++nex;
-      if (ds > 0) out[2]++;
-      int key[4];
-      for (int i = 0; i < nv; ++i) key[i] = v[i];
-      if (insphere_sos(dim, q, key, e, opp, nullptr, nullptr) > 0) out[3]++;
     }
-  }
+    part[tid] = c;
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nth; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& x : th) x.join();
+  for (const auto& c : part)
+    for (int i = 0; i < 8; ++i) out[i] += c[i];
+  std::vector<char> seen(nvert, 0);
+  for (int64_t s = 0; s < ns; ++s)
+    for (int i = 0; i < nv; ++i) seen[simp[4 * s + i]] = 1;
   for (int64_t i = 0; i < expect_vertices && i < nvert; ++i)
     if (!seen[i]) out[6]++;
-  out[7] = nex;
 }
 
 // Export alive simplices of an oracle handle (same layout as vdo_validate).

@@ -131,6 +131,25 @@ def test_insert_point_one_by_one(vd, oracle):
     assert np.array_equal(t.edges(), oracle.Triangulation(p).edges())
 
 
+def test_insert_point_one_by_one_3d(vd, oracle):
+    """TreeUpdate::new + insert_point (src/delaunay_tree.rs:709-740, :125-211),
+    the reference's sequential path (src/lib.rs:108-114), in 3D."""
+    p = W.uniform_points(300, 3, 19)
+    t = vd.DelaunayTree(p)
+    for q in p:
+        t.insert_point(q)
+    assert t.num_vertices == len(p)
+    assert np.array_equal(t.edges(), oracle.Triangulation(p).edges())
+    assert t.check_delaunay()
+    # then the rest of a larger set through add_points_to_tree, as the reference does past 1e5 points
+    q = W.uniform_points(5000, 3, 20)
+    t2 = vd.DelaunayTree(q)
+    for x in q[:200]:
+        t2.insert_point(x)
+    t2.add_points_to_tree(q[200:], seed=4)
+    assert np.array_equal(t2.edges(), oracle.Triangulation(q).edges())
+
+
 def test_validator_on_gpu_simplices(vd, oracle):
     p = W.uniform_points(4000, 3, 31)
     t, _ = gpu_edges(vd, p)

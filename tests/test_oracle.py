@@ -164,3 +164,21 @@ def test_parallel_reference_path_same_triangulation(oracle, dim, n, prefix):
     b = oracle.Triangulation(p, seed=3, threads=4, prefix=prefix)
     assert a.status == 0 and b.status == 0
     assert np.array_equal(a.edges(), b.edges())
+
+
+def test_big_golden_digest_of_c1_reproduces(oracle):
+    """The committed full-size digests come from tests/golden/make_big_golden.py;
+    its 10k-point 2D entry is recomputed here from the oracle."""
+    import importlib.util
+    import json
+    import os
+    gdir = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location("make_big_golden", os.path.join(gdir, "make_big_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    with open(os.path.join(gdir, "big_edges.json")) as f:
+        table = json.load(f)
+    p = m.workloads()["c1"]()
+    rows, sha = m.digest(oracle.Triangulation(p, seed=1).edges())
+    assert (rows, sha) == (table["c1"]["edges"], table["c1"]["sha256"])
+    assert set(table) >= {"c1", "c2", "c3", "u2"}

@@ -58,3 +58,43 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(vd):
     assert rc == 1  # VD_ERR_ARG: more simplices than the static scratch holds
     rc, _ = _noalloc(L, 3, dummy, 1, 65536 + 1, dummy, 4)
     assert rc == 1  # VD_ERR_ARG: vertex ids beyond the static scratch
+
+
+def test_noalloc_long_bucket_fan_matches_numpy(vd):
+    """Vertex 0 in 1,500 tetrahedra: its bucket (4,500 entries, most of them
+    repeated edges) is longer than one warp sorts, so the block-per-bucket
+    path runs; the result must equal np.unique of the same edges."""
+    import torch
+    from voronoids_gb300 import _native
+    L = _native.load()
+    k = 1500
+    i = np.arange(1, k + 1)
+    tets = np.stack([np.zeros(k, np.int64), i, i + 1, i + 2], axis=1)
+    nverts = k + 3
+    pairs = np.concatenate([np.sort(tets[:, [a, b]], axis=1) for a in range(4) for b in range(a + 1, 4)])
+    want = np.unique(pairs, axis=0)
+    simp = torch.from_numpy(tets.astype(np.int32)).cuda()
+    cap = len(pairs)
+    for call in range(2):
+        out = torch.full((2 * cap,), -1, dtype=torch.int32, device="cuda")
+        rc, m = _noalloc(L, 3, simp, k, nverts, out, cap)
+        assert rc == 0, (call, rc)
+        got = out[: 2 * m].view(-1, 2).cpu().numpy().astype(np.int64)
+        assert np.array_equal(got, want), call
+
+
+def test_noalloc_reports_bad_ids_and_short_output(vd):
+    import torch
+    from voronoids_gb300 import _native
+    L = _native.load()
+    tets = np.array([[0, 1, 2, 3], [1, 2, 3, 4]], dtype=np.int32)
+    simp = torch.from_numpy(tets).cuda()
+    out = torch.zeros(64, dtype=torch.int32, device="cuda")
+    rc, m = _noalloc(L, 3, simp, 2, 5, out, 32)
+    assert rc == 0 and m == 9
+    rc, m = _noalloc(L, 3, simp, 2, 5, out, 4)
+    assert rc == 1 and m == 9  # VD_ERR_ARG: output too short; the count is still reported
+    rc, m = _noalloc(L, 3, simp, 2, 4, out, 32)
+    assert rc == 1  # VD_ERR_ARG: vertex id 4 is not below nverts = 4
+    rc, m = _noalloc(L, 3, simp, 2, 5, out, 32)
+    assert rc == 0 and m == 9  # a good call after the rejected ones

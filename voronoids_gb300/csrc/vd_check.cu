@@ -11,6 +11,7 @@
 // Locally Delaunay everywhere implies globally Delaunay (Delaunay's lemma).
 #include <cuda_runtime.h>
 
+#include "../../include/voronoids_gpu.h"
 #include "vd_common.cuh"
 
 namespace vd {
@@ -76,6 +77,52 @@ __global__ void k_check(DevTree T, int nsimp, unsigned long long* out) {
   if (perr) set_error(T.ctr, E_PRECISION);
 }
 
+// Caller triangulation -> device records: vertex i of `xyz` (dim doubles) as
+// a 32-byte (x, y, z | 0, 0) record.
+template <int D>
+__global__ void k_pack_points(const double* xyz, long long n, double4_32a* out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = make_double4_32a(xyz[i * D], xyz[i * D + 1], D == 3 ? xyz[i * D + 2] : 0.0, 0.0);
+}
+
+// Plain neighbour ids -> face codes (o << 2 | g, g the face of o whose
+// neighbour is s).  A structural fault is kept visible to k_check instead of
+// being repaired: a vertex id outside [0, npts) becomes npts (k_check counts
+// it as a structural violation), a neighbour id outside [0, ns) becomes the
+// out-of-range code ns << 2, and a neighbour with no face pointing back gets
+// a face whose link does not point back either (counted as asymmetric).
+template <int D>
+__global__ void k_face_codes(const int4* verts, const int4* nbrs, int ns, int npts, Simplex* out) {
+  constexpr int NV = D + 1;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+    const int4 v = verts[s], n = nbrs[s];
+    int va[4] = {v.x, v.y, v.z, v.w}, na[4] = {n.x, n.y, n.z, n.w}, code[4] = {-1, -1, -1, -1};
+    for (int j = 0; j < NV; ++j)
+      if (va[j] < 0 || va[j] >= npts) va[j] = npts;
+    if (D == 2) va[3] = -1;
+    for (int f = 0; f < NV; ++f) {
+      const int o = na[f];
+      if (o == -1) continue;
+      if (o < 0 || o >= ns) {
+        code[f] = ns << 2;
+        continue;
+      }
+      const int4 b = nbrs[o];
+      const int ba[4] = {b.x, b.y, b.z, b.w};
+      int g = 0;
+      while (g < NV && ba[g] != s) ++g;
+      if (g == NV) g = 0;  // no face of o points back, so neither does face 0
+      code[f] = (o << 2) | g;
+    }
+    Simplex r;
+    for (int j = 0; j < 4; ++j) {
+      r.v[j] = va[j];
+      r.n[j] = code[j];
+    }
+    out[s] = r;
+  }
+}
+
 }  // namespace
 
 void launch_check(const DevTree& T, const Launch& L, int dim, int nsimp, unsigned long long* d_out) {
@@ -88,3 +135,87 @@ void launch_check(const DevTree& T, const Launch& L, int dim, int nsimp, unsigne
 }
 
 }  // namespace vd
+
+// ---------------------------------------------------------------------------
+// check_delaunay on a caller's triangulation (see include/voronoids_gpu.h).
+extern "C" int vd_check_triangulation(int dim, const double* pts, int64_t npts, const int32_t* verts,
+                                      const int32_t* nbrs, int64_t ns, int* ok, int64_t* violations) {
+  using namespace vd;
+  if ((dim != 2 && dim != 3) || !ok || npts < 0 || ns < 0 || npts > 0x7ffffff0LL || ns >= (int64_t(1) << 29) ||
+      (npts > 0 && !pts) || (ns > 0 && (!verts || !nbrs)))
+    return VD_ERR_ARG;
+  *ok = 0;
+  int dev = 0, sms = 1;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return VD_ERR_CUDA;
+  double* d_xyz = nullptr;
+  double4_32a* d_pts = nullptr;
+  int4 *d_v = nullptr, *d_n = nullptr;
+  Simplex* d_simp = nullptr;
+  Counters* d_ctr = nullptr;
+  unsigned long long* d_out = nullptr;
+  cudaStream_t st = nullptr;
+  int rc = VD_OK;
+  const size_t np = (size_t)std::max<int64_t>(npts, 1), nsz = (size_t)std::max<int64_t>(ns, 1);
+  if (cudaMalloc((void**)&d_xyz, sizeof(double) * dim * np) != cudaSuccess ||
+      cudaMalloc((void**)&d_pts, sizeof(double4_32a) * np) != cudaSuccess ||
+      cudaMalloc((void**)&d_v, sizeof(int4) * nsz) != cudaSuccess ||
+      cudaMalloc((void**)&d_n, sizeof(int4) * nsz) != cudaSuccess ||
+      cudaMalloc((void**)&d_simp, sizeof(Simplex) * nsz) != cudaSuccess ||
+      cudaMalloc((void**)&d_ctr, sizeof(Counters)) != cudaSuccess ||
+      cudaMalloc((void**)&d_out, 6 * sizeof(unsigned long long)) != cudaSuccess)
+    rc = VD_ERR_NOMEM;
+  if (rc == VD_OK && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) rc = VD_ERR_CUDA;
+  unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
+  Counters hc;
+  memset(&hc, 0, sizeof(hc));
+  if (rc == VD_OK) {
+    bool good = cudaMemsetAsync(d_ctr, 0, sizeof(Counters), st) == cudaSuccess;
+    if (npts > 0)
+      good = good && cudaMemcpyAsync(d_xyz, pts, sizeof(double) * dim * npts, cudaMemcpyHostToDevice, st) == cudaSuccess;
+    if (ns > 0)
+      good = good && cudaMemcpyAsync(d_v, verts, sizeof(int4) * ns, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+             cudaMemcpyAsync(d_n, nbrs, sizeof(int4) * ns, cudaMemcpyHostToDevice, st) == cudaSuccess;
+    Launch L;
+    L.blocks = sms * 8;
+    L.warps = sms * 20;
+    L.stream = st;
+    if (good) {
+      note_launches(2);
+      if (dim == 3) {
+        k_pack_points<3><<<L.blocks, 256, 0, st>>>(d_xyz, npts, d_pts);
+        k_face_codes<3><<<L.blocks, 256, 0, st>>>(d_v, d_n, (int)ns, (int)npts, d_simp);
+      } else {
+        k_pack_points<2><<<L.blocks, 256, 0, st>>>(d_xyz, npts, d_pts);
+        k_face_codes<2><<<L.blocks, 256, 0, st>>>(d_v, d_n, (int)ns, (int)npts, d_simp);
+      }
+      DevTree T;
+      memset(&T, 0, sizeof(T));
+      T.pts = reinterpret_cast<vdp::VPt*>(d_pts);
+      T.simp = d_simp;
+      T.ctr = d_ctr;
+      T.nsets = 1;
+      T.cap_simp = (int)ns;
+      T.cap_verts = (int)npts;
+      launch_check(T, L, dim, (int)ns, d_out);
+      good = cudaGetLastError() == cudaSuccess &&
+             cudaMemcpyAsync(h, d_out, sizeof(h), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+             cudaMemcpyAsync(&hc, d_ctr, sizeof(hc), cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess || !good) rc = VD_ERR_CUDA;
+  }
+  if (st) cudaStreamDestroy(st);
+  cudaFree(d_xyz);
+  cudaFree(d_pts);
+  cudaFree(d_v);
+  cudaFree(d_n);
+  cudaFree(d_simp);
+  cudaFree(d_ctr);
+  cudaFree(d_out);
+  if (rc != VD_OK) return rc;
+  if (violations)
+    for (int k = 0; k < 6; ++k) violations[k] = (int64_t)h[k];
+  *ok = (h[0] == 0 && h[1] == 0 && h[2] == 0 && h[3] == 0) ? 1 : 0;
+  return hc.err ? hc.err : VD_OK;
+}

@@ -2,7 +2,7 @@
 // as input-index pairs (u < v), sorted lexicographically.
 //
 // The reference exposes the graph only through its simplex map
-// (PyDelauanyTree.simplices, src/lib.rs:142-156); the parity contract of this
+// (PyDelauanyTree.simplices, src/lib.rs:87-100); the parity contract of this
 // build is the sorted edge list derived from it.  Instead of a global sort of
 // all (simplex, edge) instances, instances are bucketed by their smaller
 // endpoint (counting pass + exclusive scan + scatter), each bucket (about 40

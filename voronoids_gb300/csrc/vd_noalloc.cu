@@ -21,8 +21,11 @@
 // overlaps (different streams or threads without ordering between them)
 // race on the array and produce garbage.  The first call on each device
 // looks up the array's device address with cudaGetSymbolAddress while that
-// device is current; make that first call before starting any stream
-// capture on the device.
+// device is current (again after the device's context has been recreated,
+// e.g. by cudaDeviceReset); make that first call before starting any stream
+// capture on the device.  Every call waits for its own work on its stream
+// to finish before it returns.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -243,21 +246,64 @@ __global__ void k_na_out(int nv, const int* S, uint2* out, long long cap) {
   }
 }
 
-// Device address of g_na_scratch, looked up once per device.
+// Device address of g_na_scratch per device, remembered together with the id
+// of the CUDA context it was looked up in.  The address belongs to the
+// module loaded in that context: after cudaDeviceReset (or any other end of
+// the device's primary context) the module is loaded again and the array may
+// sit elsewhere, so a new context id means a new lookup.  Context ids come
+// from the driver API (cuCtxGetCurrent, cuCtxGetId), reached through the
+// runtime's driver entry points so that the library needs no libcuda link.
 constexpr int kNaMaxDevices = 64;
-int* g_na_addr[kNaMaxDevices] = {};
+struct NaSlot {
+  unsigned long long ctx_id;
+  int* addr;
+};
+NaSlot g_na_slot[kNaMaxDevices] = {};
 std::mutex g_na_mutex;
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// Id of the calling thread's current context, 0 if none or unknown.
+unsigned long long current_ctx_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 int na_scratch(int** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return VD_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (!g_na_addr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_na_scratch) != cudaSuccess || !p) return VD_ERR_CUDA;
-    g_na_addr[dev] = static_cast<int*>(p);
+  NaSlot& slot = g_na_slot[dev];
+  const unsigned long long id = current_ctx_id();
+  if (id != 0 && slot.addr && slot.ctx_id == id) {
+    *out = slot.addr;
+    return VD_OK;
   }
-  *out = g_na_addr[dev];
+  // first call on this device, or a new context: look the address up with
+  // the device current (this may also make the primary context current)
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_na_scratch) != cudaSuccess || !p) return VD_ERR_CUDA;
+  slot.addr = static_cast<int*>(p);
+  slot.ctx_id = current_ctx_id();  // 0 (unknown): looked up again on the next call
+  *out = slot.addr;
   return VD_OK;
 }
 
@@ -274,8 +320,9 @@ extern "C" int vd_edges_from_simplices_noalloc(int dim, const int32_t* d_simp, i
   cudaStream_t st = (cudaStream_t)stream;
   const int nv = (int)nverts;
   // zero what the call counts into: bucket counts and the control words
-  cudaMemsetAsync(S + kNaCnt, 0, sizeof(int) * (nv + 1), st);
-  cudaMemsetAsync(S + kNaCtl, 0, sizeof(int) * 16, st);
+  if (cudaMemsetAsync(S + kNaCnt, 0, sizeof(int) * (nv + 1), st) != cudaSuccess ||
+      cudaMemsetAsync(S + kNaCtl, 0, sizeof(int) * 16, st) != cudaSuccess)
+    return VD_ERR_CUDA;
   const int blocks = 1024;
   k_na_count<<<blocks, 256, 0, st>>>(d_simp, ns, nv, dim, S);
   k_na_scan<<<1, 1024, 0, st>>>(S + kNaCnt, S + kNaOff, nv);
@@ -285,10 +332,14 @@ extern "C" int vd_edges_from_simplices_noalloc(int dim, const int32_t* d_simp, i
   k_na_scan<<<1, 1024, 0, st>>>(S + kNaUcnt, S + kNaUoff, nv);
   k_na_out<<<blocks, 256, 0, st>>>(nv, S, reinterpret_cast<uint2*>(d_uv), cap);
   vd::note_launches(7);
+  // launch errors of this call, read without clearing an error the caller's
+  // thread may hold from before
+  if (cudaPeekAtLastError() != cudaSuccess) return VD_ERR_CUDA;
   int host[2] = {0, 0};
-  cudaMemcpyAsync(&host[0], S + kNaUoff + nv, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(&host[1], S + kNaCtl + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return VD_ERR_CUDA;
+  if (cudaMemcpyAsync(&host[0], S + kNaUoff + nv, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&host[1], S + kNaCtl + 1, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return VD_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return VD_ERR_CUDA;
   *n_edges = host[0];
   if (host[1]) return VD_ERR_ARG;  // a vertex id was >= nverts
   return host[0] > cap ? VD_ERR_ARG : VD_OK;

@@ -335,6 +335,30 @@ class DelaunayTree:
         return {k: getattr(s, k) for k, _ in s._fields_}
 
 
+def check_triangulation(points, verts, nbrs):
+    """``check_delaunay`` on a caller's triangulation (``vd_check_triangulation``).
+
+    ``points`` (npts, dim) are the vertices by id (any super vertices
+    included), ``verts`` (ns, 4) int32 vertex ids oriented as
+    :meth:`DelaunayTree.simplices` exports them, ``nbrs`` (ns, 4) the simplex
+    across the face opposite each vertex (-1 on the hull).  Returns
+    ``(ok, violations)``; the violations are counted on the GPU exactly as
+    :meth:`DelaunayTree.check_delaunay` counts them."""
+    p = _points(points)
+    v = np.ascontiguousarray(verts, dtype=np.int32)
+    nb = np.ascontiguousarray(nbrs, dtype=np.int32)
+    if v.ndim != 2 or v.shape[1] != 4 or nb.shape != v.shape:
+        raise ValueError("verts and nbrs must both have shape (ns, 4)")
+    ok = ctypes.c_int(0)
+    viol = (ctypes.c_int64 * 6)()
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    _check(_native.load().vd_check_triangulation(p.shape[1], _dp(p), p.shape[0], v.ctypes.data_as(i32p),
+                                                 nb.ctypes.data_as(i32p), v.shape[0], ctypes.byref(ok), viol),
+           "check_triangulation")
+    keys = ["non_positive", "asymmetric", "not_delaunay", "not_perturbed_delaunay", "hull_facets", "facets"]
+    return bool(ok.value), dict(zip(keys, list(viol)))
+
+
 def delaunay(points, seed=0):
     """``voronoids.delaunay(points)``: new(points) + insert all points.
 
