@@ -53,6 +53,13 @@ def lib():
         L.vdo_simplices.restype = ctypes.c_int64
         L.vdo_validate.argtypes = [ctypes.c_int, dp, ctypes.c_int64, i32p, i32p,
                                    ctypes.c_int64, ctypes.c_int64, llp]
+        L.vdo_build_float.argtypes = [ctypes.c_int, dp, ctypes.c_int64, llp]
+        L.vdo_build_float.restype = ctypes.c_void_p
+        L.vdo_float_edges.argtypes = [ctypes.c_void_p, i64p, ctypes.c_int64]
+        L.vdo_float_edges.restype = ctypes.c_int64
+        L.vdo_float_export.argtypes = [ctypes.c_void_p, dp, i32p, i32p, llp]
+        L.vdo_float_export.restype = ctypes.c_int64
+        L.vdo_float_free.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -199,3 +206,47 @@ def validate(dim, verts, simp, nbr, expect_vertices=0):
     keys = ["non_positive", "asymmetric", "not_delaunay", "not_perturbed_delaunay",
             "hull_facets", "facets", "missing_vertices", "exact_calls"]
     return dict(zip(keys, list(out)))
+
+
+class FloatTriangulation:
+    """The reference's own insertion path with its floating-point conflict
+    test (circumsphere centre and radius, then ``dist^2 < r^2``), sequential
+    in input order: a diagnostic of how the reference's inexact decisions
+    differ from the exact triangulation.  See ``vdo_build_float``."""
+
+    def __init__(self, points):
+        p = _c(points, np.float64)
+        self.dim = p.shape[1]
+        st = (ctypes.c_longlong * 8)()
+        self._h = lib().vdo_build_float(self.dim, _dp(p), p.shape[0], st)
+        if not self._h:
+            raise ValueError("bad input")
+        keys = ["inserted", "empty_located", "malformed_new", "max_killed", "live_simplices", "vertices"]
+        self.stats = dict(zip(keys, list(st)[:6]))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().vdo_float_free(self._h)
+            self._h = None
+
+    def edges(self):
+        L = lib()
+        m = L.vdo_float_edges(self._h, None, 0)
+        out = np.zeros((m, 2), dtype=np.int64)
+        L.vdo_float_edges(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), m)
+        return out
+
+    def export(self):
+        """(verts (nv, 3), simplices (ns, 4) int32, neighbours (ns, 4) int32,
+        links that could not be placed on a face) in ``validate``'s layout."""
+        L = lib()
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        ns = L.vdo_float_export(self._h, None, None, None, None)
+        nv = self.stats["vertices"] - (self.dim + 1)
+        verts = np.zeros((nv, 3))
+        simp = np.zeros((ns, 4), dtype=np.int32)
+        nbr = np.zeros((ns, 4), dtype=np.int32)
+        bad = ctypes.c_longlong(0)
+        L.vdo_float_export(self._h, _dp(verts), simp.ctypes.data_as(i32p), nbr.ctypes.data_as(i32p),
+                           ctypes.byref(bad))
+        return verts, simp, nbr, int(bad.value)

@@ -461,8 +461,12 @@ void super_vertices(int dim, const double* pts, int64_t n, double* out, double* 
   }
 }
 
-// Float variant of the reference circumsphere (src/geometry.rs:2-56): 2D slope
-// formula, 3D Gaussian elimination with partial pivoting.
+// Float variant of the reference circumsphere (src/geometry.rs:2-56): the 2D
+// slope formula; in 3D the system `direction * c = planes` solved as
+// nalgebra 0.32.4's LU does it (restated from its published algorithm:
+// partial pivoting on the first largest |a| of the column, multipliers scaled
+// by the reciprocal of the pivot, unit lower triangular forward solve,
+// column-oriented upper triangular back solve), then the radius to vertex 0.
 void circumsphere_float(int dim, const double* v, double* center, double* radius) {
   if (dim == 2) {
     double x1 = v[0], y1 = v[1], x2 = v[2], y2 = v[3], x3 = v[4], y3 = v[5];
@@ -483,37 +487,36 @@ void circumsphere_float(int dim, const double* v, double* center, double* radius
     double s = 0.0;
     for (int j = 0; j < 3; ++j) {
       A[i][j] = v[(i + 1) * 3 + j] - v[j];
-      double mid = (v[(i + 1) * 3 + j] + v[j]) / 2.0;
-      s += A[i][j] * mid;
+      const double mid = (v[(i + 1) * 3 + j] + v[j]) / 2.0;
+      const double t = A[i][j] * mid;
+      s = j == 0 ? t : s + t;  // column_sum: ((m0 + m1) + m2)
     }
     b[i] = s;
   }
-  int piv[3] = {0, 1, 2};
   for (int k = 0; k < 3; ++k) {
     int p = k;
     for (int i = k + 1; i < 3; ++i)
       if (std::fabs(A[i][k]) > std::fabs(A[p][k])) p = i;
+    if (A[p][k] == 0.0) continue;
     if (p != k) {
       for (int j = 0; j < 3; ++j) std::swap(A[k][j], A[p][j]);
       std::swap(b[k], b[p]);
-      std::swap(piv[k], piv[p]);
     }
-    for (int i = k + 1; i < 3; ++i) {
-      double f = A[i][k] / A[k][k];
-      for (int j = k; j < 3; ++j) A[i][j] -= f * A[k][j];
-      b[i] -= f * b[k];
-    }
+    const double inv = 1.0 / A[k][k];
+    for (int i = k + 1; i < 3; ++i) A[i][k] *= inv;
+    for (int j = k + 1; j < 3; ++j)
+      for (int i = k + 1; i < 3; ++i) A[i][j] = A[i][j] + (-A[k][j]) * A[i][k];
   }
-  double xs[3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = i + 1; j < 3; ++j) b[j] = b[j] + (-b[i]) * A[j][i];
   for (int i = 2; i >= 0; --i) {
-    double s = b[i];
-    for (int j = i + 1; j < 3; ++j) s -= A[i][j] * xs[j];
-    xs[i] = s / A[i][i];
+    const double x = b[i] / A[i][i];
+    b[i] = x;
+    for (int k = 0; k < i; ++k) b[k] = b[k] + (-x) * A[k][i];
   }
-  for (int j = 0; j < 3; ++j) center[j] = xs[j];
-  double r2 = 0.0;
-  for (int j = 0; j < 3; ++j) r2 += (v[j] - xs[j]) * (v[j] - xs[j]);
-  *radius = std::sqrt(r2);
+  for (int j = 0; j < 3; ++j) center[j] = b[j];
+  const double dx = v[0] - b[0], dy = v[1] - b[1], dz = v[2] - b[2];
+  *radius = std::sqrt(dx * dx + dy * dy + dz * dz);
 }
 
 // Insertion priority: a bijective 32-bit mix of the vertex id and the seed.
@@ -1064,6 +1067,329 @@ int build_parallel(Tree& t, int64_t n, int threads, int64_t prefix) {
   return OK;
 }
 
+// ---------------------------------------------------------------------------
+// The reference's own floating-point semantics (diagnostic, not the parity
+// contract).  A sequential restatement of the reference's insertion path with
+// its data model and its inexact conflict test, used to count how often that
+// test decides differently from the exact one:
+//   DelaunayTree::new super + ghost simplices  src/delaunay_tree.rs:389-510, :544-640
+//   locate / find_all_neighbors                :33-75 (the nearest vertex's
+//                                              simplices, then every conflicting
+//                                              simplex reached from them)
+//   get_new_simplices                          :77-123
+//   insert_point                               :125-211
+//   pair_simplices, TreeUpdate::new            :674-740
+//   circumsphere_2d / _3d, in_sphere           src/geometry.rs:2-97
+// The nearest vertex comes from a uniform grid instead of the kiddo 4.2.0
+// kd-tree; equal distances go to the smallest vertex id (kiddo's own tie rule
+// is not pinned).  A point whose located set is empty (the reference panics,
+// :53) is counted and skipped.
+// ---------------------------------------------------------------------------
+struct RSimplex {
+  int v[4];
+  double c[3];
+  double r;
+  std::vector<int> nb;  // unordered neighbour ids, as the reference keeps them
+  bool alive;
+};
+
+// Circumsphere of the reference (src/geometry.rs:2-56) over the dim
+// coordinates of the vertices, in the order the simplex lists them.
+void ref_circumsphere(int dim, const P3* q, double* c, double* r) {
+  double v[12];
+  for (int j = 0; j <= dim; ++j) {
+    const double x[3] = {q[j].x, q[j].y, q[j].z};
+    for (int k = 0; k < dim; ++k) v[j * dim + k] = x[k];
+  }
+  circumsphere_float(dim, v, c, r);
+}
+
+bool ref_conflict(int dim, const P3& p, const RSimplex& s) {
+  const double v[3] = {p.x, p.y, p.z};
+  return rs_in_sphere(v, s.c, s.r, dim);
+}
+
+// Nearest vertex by a uniform grid over the input box; vertices outside the
+// box (super and ghost vertices) are checked one by one.
+struct NNGrid {
+  int dim = 3, side = 1;
+  double lo[3] = {0, 0, 0}, w[3] = {1, 1, 1};
+  std::vector<std::vector<int>> cell;
+  std::vector<int> far;
+  void init(int d, const std::vector<P3>& in, int64_t n) {
+    dim = d;
+    double hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    lo[0] = lo[1] = lo[2] = INFINITY;
+    for (const P3& p : in) {
+      const double c[3] = {p.x, p.y, p.z};
+      for (int k = 0; k < dim; ++k) {
+        lo[k] = std::min(lo[k], c[k]);
+        hi[k] = std::max(hi[k], c[k]);
+      }
+    }
+    side = std::max(1, (int)std::floor(std::pow(std::max<double>(1.0, (double)n / 2.0), 1.0 / dim)));
+    side = std::min(side, dim == 3 ? 256 : 2048);
+    for (int k = 0; k < 3; ++k) {
+      if (k >= dim) {
+        lo[k] = 0;
+        w[k] = 1;
+        continue;
+      }
+      w[k] = std::max((hi[k] - lo[k]) / side, 1e-300);
+    }
+    cell.assign((size_t)std::pow(side, dim), {});
+  }
+  bool cell_of(const P3& p, int* ic) const {
+    const double c[3] = {p.x, p.y, p.z};
+    bool inside = true;
+    for (int k = 0; k < 3; ++k) {
+      if (k >= dim) {
+        ic[k] = 0;
+        continue;
+      }
+      const double u = (c[k] - lo[k]) / w[k];
+      if (!(u >= 0.0) || u > (double)side) inside = false;
+      ic[k] = u < 0.0 ? 0 : (u >= side ? side - 1 : (int)u);
+    }
+    return inside;
+  }
+  size_t index(const int* ic) const {
+    size_t i = 0;
+    for (int k = dim - 1; k >= 0; --k) i = i * side + ic[k];
+    return i;
+  }
+  void add(int id, const P3& p) {
+    int ic[3];
+    if (cell_of(p, ic))
+      cell[index(ic)].push_back(id);
+    else
+      far.push_back(id);
+  }
+  int nearest(const P3& p, const std::vector<P3>& pts) const {
+    double best = INFINITY;
+    int bi = -1;
+    auto test = [&](int id) {
+      const P3& q = pts[id];
+      double d = (p.x - q.x) * (p.x - q.x) + (p.y - q.y) * (p.y - q.y);
+      if (dim == 3) d += (p.z - q.z) * (p.z - q.z);
+      if (d < best || (d == best && id < bi)) {
+        best = d;
+        bi = id;
+      }
+    };
+    for (int id : far) test(id);
+    int ic[3];
+    cell_of(p, ic);
+    const double c[3] = {p.x, p.y, p.z};
+    for (int r = 0; r <= side; ++r) {
+      int a[3], b[3];
+      for (int k = 0; k < 3; ++k) {
+        a[k] = k < dim ? std::max(0, ic[k] - r) : 0;
+        b[k] = k < dim ? std::min(side - 1, ic[k] + r) : 0;
+      }
+      for (int z = a[2]; z <= b[2]; ++z)
+        for (int y = a[1]; y <= b[1]; ++y)
+          for (int x = a[0]; x <= b[0]; ++x) {
+            const int cc[3] = {x, y, z};
+            int cheb = 0;
+            for (int k = 0; k < dim; ++k) cheb = std::max(cheb, std::abs(cc[k] - ic[k]));
+            if (cheb != r) continue;
+            for (int id : cell[index(cc)]) test(id);
+          }
+      // any vertex in a later ring is at least this far from p
+      double gap = INFINITY;
+      for (int k = 0; k < dim; ++k) {
+        gap = std::min(gap, c[k] - (lo[k] + (ic[k] - r) * w[k]));
+        gap = std::min(gap, (lo[k] + (ic[k] + r + 1) * w[k]) - c[k]);
+      }
+      if (bi >= 0 && gap > 0 && best <= gap * gap) break;
+    }
+    return bi;
+  }
+};
+
+struct RTree {
+  int dim = 3, M = 4;
+  std::vector<P3> pts;
+  std::vector<std::vector<int>> vsimp;
+  std::vector<RSimplex> s;
+  int64_t max_id = 0;
+  NNGrid grid;
+  std::vector<int> mark;
+  int stamp = 0;
+  long long inserted = 0, empty = 0, malformed = 0, max_killed = 0;
+};
+
+// DelaunayTree::new (src/delaunay_tree.rs:389-510 3D, :544-640 2D): super
+// vertices, ghost vertices, the super simplex with the bounding sphere
+// (centre, 10 r) as its sphere, and radius-0 ghost simplices on its faces.
+void ref_new(RTree& t, int dim, const double* in, int64_t n) {
+  t.dim = dim;
+  t.M = dim + 1;
+  double cen[3] = {0, 0, 0}, r;
+  bounding_sphere(dim, in, n, cen, &r);
+  double sv[4][3] = {};
+  double R;
+  super_vertices(dim, in, n, &sv[0][0], &R);
+  if (dim == 3) {
+    for (int i = 0; i < 4; ++i) t.pts.push_back({sv[i][0], sv[i][1], sv[i][2]});
+    const P3 top{cen[0], cen[1], R + cen[2]};
+    t.pts.push_back(top);
+    t.pts.push_back(top);
+    t.pts.push_back(top);
+    t.pts.push_back({cen[0] + R, cen[1], cen[2] - R});
+    t.vsimp = {{0, 1, 2, 3}, {0, 1, 3, 4}, {0, 1, 2, 4}, {0, 2, 3, 4}, {1}, {2}, {3}, {4}};
+    const int sv_ids[5][4] = {{0, 1, 2, 3}, {4, 0, 1, 2}, {5, 0, 2, 3}, {6, 0, 3, 1}, {7, 1, 2, 3}};
+    for (int k = 0; k < 5; ++k) {
+      RSimplex S{};
+      for (int j = 0; j < 4; ++j) S.v[j] = sv_ids[k][j];
+      S.alive = true;
+      if (k == 0) {
+        S.c[0] = cen[0];
+        S.c[1] = cen[1];
+        S.c[2] = cen[2];
+        S.r = R;
+        S.nb = {1, 2, 3, 4};
+      } else {
+        S.r = 0.0;
+        S.nb = {0};
+      }
+      t.s.push_back(S);
+    }
+    t.max_id = 4;
+  } else {
+    for (int i = 0; i < 3; ++i) t.pts.push_back({sv[i][0], sv[i][1], 0.0});
+    for (int i = 0; i < 3; ++i) t.pts.push_back({sv[i][0], sv[i][1], 0.0});
+    t.vsimp = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1}, {2}, {3}};
+    const int sv_ids[4][3] = {{0, 1, 2}, {3, 0, 1}, {4, 0, 2}, {5, 1, 2}};
+    for (int k = 0; k < 4; ++k) {
+      RSimplex S{};
+      for (int j = 0; j < 3; ++j) S.v[j] = sv_ids[k][j];
+      S.v[3] = -1;
+      S.alive = true;
+      if (k == 0) {
+        S.c[0] = cen[0];
+        S.c[1] = cen[1];
+        S.r = R;
+        S.nb = {1, 2, 3};
+      } else {
+        S.r = 0.0;
+        S.nb = {0};
+      }
+      t.s.push_back(S);
+    }
+    t.max_id = 3;
+  }
+  std::vector<P3> box;
+  for (int64_t k = 0; k < n; ++k) box.push_back({in[k * dim], in[k * dim + 1], dim == 3 ? in[k * dim + 2] : 0.0});
+  t.grid.init(dim, box, n);
+  for (int id = 0; id < (int)t.pts.size(); ++id) t.grid.far.push_back(id);
+}
+
+// TreeUpdate::new + insert_point for vertex `vid` (already in t.pts).
+void ref_insert(RTree& t, int vid) {
+  const P3 p = t.pts[vid];
+  const int M = t.M, N = t.dim;
+  if (t.mark.size() < t.s.size() + 64) t.mark.resize(2 * t.s.size() + 64, 0);
+  ++t.stamp;
+  // locate: the nearest vertex's simplices, then find_all_neighbors from
+  // each one in conflict
+  const int nn = t.grid.nearest(p, t.pts);
+  std::vector<int> out;
+  std::vector<int> stack;
+  for (int id : t.vsimp[nn]) {
+    if (!ref_conflict(N, p, t.s[id])) continue;
+    if (t.mark[id] != t.stamp) {
+      t.mark[id] = t.stamp;
+      out.push_back(id);
+    }
+    stack.push_back(id);
+    while (!stack.empty()) {
+      const int node = stack.back();
+      stack.pop_back();
+      for (int nb : t.s[node].nb) {
+        if (t.mark[nb] == t.stamp || !ref_conflict(N, p, t.s[nb])) continue;
+        t.mark[nb] = t.stamp;
+        out.push_back(nb);
+        stack.push_back(nb);
+      }
+    }
+  }
+  if (out.empty()) {  // the reference panics here (src/delaunay_tree.rs:53)
+    ++t.empty;
+    return;
+  }
+  std::sort(out.begin(), out.end());
+  t.max_killed = std::max<long long>(t.max_killed, (long long)out.size());
+  // get_new_simplices for every killed simplex
+  struct New {
+    int v[4];
+    int outer, killed;
+  };
+  std::vector<New> nw;
+  for (int k : out) {
+    const RSimplex& K = t.s[k];
+    for (int nb : K.nb) {
+      const RSimplex& B = t.s[nb];
+      if (ref_conflict(N, p, B)) continue;
+      New x{{vid, 0, 0, 0}, nb, k};
+      if (N == 2) x.v[3] = -1;
+      int count = 1;
+      for (int i = 0; i < M; ++i) {
+        bool in_k = false;
+        for (int j = 0; j < M; ++j) in_k = in_k || K.v[j] == B.v[i];
+        if (in_k) {
+          if (count < M) x.v[count] = B.v[i];
+          ++count;
+        }
+      }
+      if (count != M) ++t.malformed;
+      nw.push_back(x);
+    }
+  }
+  // pair_simplices: new simplices sharing N vertices are neighbours
+  const int64_t base = t.max_id;
+  t.s.resize(base + 1 + nw.size());
+  for (size_t i = 0; i < nw.size(); ++i) {
+    RSimplex& S = t.s[base + 1 + i];
+    P3 q[4];
+    for (int j = 0; j < M; ++j) {
+      S.v[j] = nw[i].v[j];
+      q[j] = t.pts[nw[i].v[j]];
+    }
+    S.v[3] = N == 2 ? -1 : S.v[3];
+    ref_circumsphere(N, q, S.c, &S.r);
+    S.nb = {nw[i].outer};
+    S.alive = true;
+  }
+  for (size_t i = 0; i < nw.size(); ++i) {
+    for (int& x : t.s[nw[i].outer].nb)
+      if (x == nw[i].killed) x = (int)(base + 1 + i);
+  }
+  for (size_t i = 0; i < nw.size(); ++i)
+    for (size_t j = i + 1; j < nw.size(); ++j) {
+      int count = 0;
+      for (int k = 0; k < M; ++k)
+        for (int l = 0; l < M; ++l) count += nw[i].v[l] == nw[j].v[k];
+      if (count == N) {
+        t.s[base + 1 + i].nb.push_back((int)(base + 1 + j));
+        t.s[base + 1 + j].nb.push_back((int)(base + 1 + i));
+      }
+    }
+  if ((int)t.vsimp.size() <= vid) t.vsimp.resize(vid + 1);
+  for (size_t i = 0; i < nw.size(); ++i)
+    for (int j = 0; j < M; ++j) t.vsimp[nw[i].v[j]].push_back((int)(base + 1 + i));
+  for (int k : out)
+    for (int i = 0; i < M; ++i) {
+      auto& l = t.vsimp[t.s[k].v[i]];
+      l.erase(std::remove(l.begin(), l.end(), k), l.end());
+    }
+  for (int k : out) t.s[k].alive = false;
+  t.max_id += (int64_t)nw.size();
+  t.grid.add(vid, p);
+  ++t.inserted;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1443,5 +1769,131 @@ int64_t vdo_simplices(void* h, int32_t* simp, int32_t* nbr) {
 }
 
 int vdo_status(void* h) { return ((Tree*)h)->status; }
+
+
+// ---- the reference's float semantics (diagnostic) --------------------------
+// Sequential insertion of all n points in input order with the reference's
+// inexact conflict test.  stats (NULL or 8): inserted, empty located sets
+// (skipped; the reference panics), new simplices whose outer neighbour did not
+// share a facet with the removed one, largest removed set, live simplices
+// (ghosts excluded), vertex count, 0, 0.
+void* vdo_build_float(int dim, const double* pts, int64_t n, long long* stats) {
+  if ((dim != 2 && dim != 3) || n < 1) return nullptr;
+  RTree* t = new RTree();
+  ref_new(*t, dim, pts, n);
+  const int first = (int)t->pts.size();
+  for (int64_t k = 0; k < n; ++k)
+    t->pts.push_back({pts[k * dim], pts[k * dim + 1], dim == 3 ? pts[k * dim + 2] : 0.0});
+  t->vsimp.resize(t->pts.size());
+  for (int64_t k = 0; k < n; ++k) ref_insert(*t, first + (int)k);
+  if (stats) {
+    long long live = 0;
+    for (const RSimplex& S : t->s) {
+      if (!S.alive) continue;
+      bool ghost = false;
+      for (int j = 0; j < t->M; ++j) ghost = ghost || (S.v[j] >= t->M && S.v[j] < 2 * t->M);
+      live += !ghost;
+    }
+    const long long v[8] = {t->inserted, t->empty, t->malformed, t->max_killed, live, (long long)t->pts.size(), 0, 0};
+    for (int i = 0; i < 8; ++i) stats[i] = v[i];
+  }
+  return t;
+}
+
+// Sorted unique edges (u < v, input numbering) of the live simplices.
+int64_t vdo_float_edges(void* h, int64_t* out, int64_t cap) {
+  RTree* t = (RTree*)h;
+  const int first = 2 * t->M;
+  std::vector<std::pair<int, int>> e;
+  for (const RSimplex& S : t->s) {
+    if (!S.alive) continue;
+    for (int i = 0; i < t->M; ++i)
+      for (int j = i + 1; j < t->M; ++j) {
+        const int a = S.v[i], b = S.v[j];
+        if (a < first || b < first || a == b) continue;
+        e.push_back({std::min(a, b) - first, std::max(a, b) - first});
+      }
+  }
+  std::sort(e.begin(), e.end());
+  e.erase(std::unique(e.begin(), e.end()), e.end());
+  if (out)
+    for (int64_t k = 0; k < (int64_t)e.size() && k < cap; ++k) {
+      out[2 * k] = e[k].first;
+      out[2 * k + 1] = e[k].second;
+    }
+  return (int64_t)e.size();
+}
+
+// The live non-ghost simplices in vdo_validate's layout: vertex ids super
+// 0..dim then the inputs, each simplex turned to positive orientation by an
+// exact orient (a degenerate one is left as it is), neighbours by face.
+// *bad counts links that cannot be placed on a face (a neighbour that is
+// dead, shares a number of vertices other than dim, or repeats a face).
+int64_t vdo_float_export(void* h, double* verts, int32_t* simp, int32_t* nbr, long long* bad) {
+  RTree* t = (RTree*)h;
+  const int M = t->M, dim = t->dim;
+  auto ghost_or_dead = [&](int id) {
+    const RSimplex& S = t->s[id];
+    if (!S.alive) return true;
+    for (int j = 0; j < M; ++j)
+      if (S.v[j] >= M && S.v[j] < 2 * M) return true;
+    return false;
+  };
+  std::vector<int> idx(t->s.size(), -1);
+  int64_t k = 0;
+  for (size_t i = 0; i < t->s.size(); ++i)
+    if (!ghost_or_dead((int)i)) idx[i] = (int)k++;
+  const int64_t nverts = (int64_t)t->pts.size() - M;
+  if (verts)
+    for (int64_t v = 0; v < nverts; ++v) {
+      const P3& q = t->pts[v < M ? v : v + M];
+      verts[3 * v] = q.x;
+      verts[3 * v + 1] = q.y;
+      verts[3 * v + 2] = q.z;
+    }
+  if (!simp) return k;
+  long long nbad = 0;
+  auto map_vertex = [&](int v) { return v < M ? v : v - M; };
+  for (size_t i = 0; i < t->s.size(); ++i) {
+    if (idx[i] < 0) continue;
+    const RSimplex& S = t->s[i];
+    int v[4] = {-1, -1, -1, -1};
+    for (int j = 0; j < M; ++j) v[j] = S.v[j];
+    P3 q[4];
+    for (int j = 0; j < M; ++j) q[j] = t->pts[v[j]];
+    if (orient(dim, q, nullptr) < 0) std::swap(v[0], v[1]);
+    int nb[4] = {-1, -1, -1, -1};
+    for (int o : S.nb) {
+      if (!t->s[o].alive) {
+        ++nbad;
+        continue;
+      }
+      if (idx[o] < 0) continue;  // a ghost: the hull
+      int missing = -1, shared = 0;
+      for (int j = 0; j < M; ++j) {
+        bool in_o = false;
+        for (int l = 0; l < M; ++l) in_o = in_o || t->s[o].v[l] == v[j];
+        if (in_o)
+          ++shared;
+        else
+          missing = j;
+      }
+      if (shared != dim || nb[missing] >= 0) {
+        ++nbad;
+        continue;
+      }
+      nb[missing] = idx[o];
+    }
+    const int64_t r = idx[i];
+    for (int j = 0; j < 4; ++j) {
+      simp[4 * r + j] = j < M ? map_vertex(v[j]) : -1;
+      nbr[4 * r + j] = nb[j];
+    }
+  }
+  if (bad) *bad = nbad;
+  return k;
+}
+
+void vdo_float_free(void* h) { delete (RTree*)h; }
 
 }  // extern "C"

@@ -182,3 +182,18 @@ def test_big_golden_digest_of_c1_reproduces(oracle):
     rows, sha = m.digest(oracle.Triangulation(p, seed=1).edges())
     assert (rows, sha) == (table["c1"]["edges"], table["c1"]["sha256"])
     assert set(table) >= {"c1", "c2", "c3", "u2"}
+
+
+def test_float_semantics_agree_with_exact_on_uniform_points(oracle):
+    """The reference's inexact path (sequential, input order) gives the exact
+    triangulation on well-spread inputs; oracle/float_diagnostic.py reports
+    where it does not."""
+    from voronoids_gb300 import workloads as W
+    for p in (W.c1_points()[:4000], W.uniform_points(3000, 3, 17)):
+        f = oracle.FloatTriangulation(p)
+        assert f.stats["inserted"] == len(p) and f.stats["empty_located"] == 0
+        assert np.array_equal(f.edges(), oracle.Triangulation(p).edges())
+        verts, simp, nbr, bad = f.export()
+        res = oracle.validate(p.shape[1], verts, simp, nbr, expect_vertices=len(verts))
+        assert bad == 0 and res["asymmetric"] == 0 and res["not_delaunay"] == 0
+
