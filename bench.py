@@ -17,7 +17,7 @@ sizing, round-parallel insertion of every point, sorted edge list.
 Between timed steps the L2 (129 MB) is flushed by writing a 256 MB buffer.
 `--impl reference` times the reference's parallel CPU path, restated in C++
 (oracle/: 1e5 sequential inserts, then 2-ring queue, greedy rounds and
-per-round parallel updates on all host threads), on a bounded sample.
+per-round parallel updates on all host threads), on the same 1M points.
 """
 import argparse
 import ctypes
@@ -37,7 +37,6 @@ sys.path.insert(0, ROOT)
 METRIC = "Mpts/s 3D 1M exact graph"
 N_POINTS = 1_000_000
 SEED = 0x5EED
-CPU_SAMPLE = 200_000
 
 # Algorithmic bytes per unit: k_cavity moves one 32-byte simplex record and
 # four 32-byte split-coordinate records per conflict test; the decide half of
@@ -56,6 +55,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_POINTS)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-subs", action="store_true", help="skip the C1 / C3 / C4-sample records of the c2 line")
     p.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
                    help="c2: 1M-point 3D build (the headline line); c3: near-degenerate 262,144 points with "
                         "predicate fallback rates; c4: 4,096 sets batched vs one set per launch; c5: Poisson "
@@ -146,12 +146,12 @@ def cpu_threads():
     return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
 
 
-def cpu_sample_desc(threads):
-    return (f"{CPU_SAMPLE} points of the same uniform 3D distribution per step: the reference's parallel path "
-            f"restated in C++ (oracle/, not the crate: no Rust toolchain here) on {threads} host threads -- "
-            f"the first {CPU_PREFIX} points inserted one at a time as src/lib.rs:108-114 does, the rest through "
-            f"2-ring queue, greedy round placement and per-round parallel updates (src/scheduler.rs, "
-            f"src/delaunay_tree.rs:336-386), exact predicates, sorted edge list")
+def cpu_sample_desc(threads, n):
+    return (f"{n} points, the full workload (1M i.i.d. uniform in [0,1)^3, splitmix64 seed 0xD1A00002), per step: "
+            f"the reference's parallel path restated in C++ (oracle/, not the crate: no Rust toolchain here) on "
+            f"{threads} host threads -- the first {CPU_PREFIX} points inserted one at a time as src/lib.rs:108-114 "
+            f"does, the rest through 2-ring queue, greedy round placement and per-round parallel updates "
+            f"(src/scheduler.rs, src/delaunay_tree.rs:336-386), exact predicates, sorted edge list")
 
 
 def cpu_build(p, threads):
@@ -162,56 +162,59 @@ def cpu_build(p, threads):
     return time.perf_counter() - t0
 
 
-def cpu_baseline():
-    """The reference's parallel CPU path (C++ restatement, all host threads) on a bounded sample."""
-    from voronoids_gb300 import workloads as W
+def cpu_baseline(pts):
+    """The reference's parallel CPU path (C++ restatement, all host threads),
+    one build of the full workload."""
     threads = cpu_threads()
-    dt = cpu_build(W.uniform_points(CPU_SAMPLE, 3, W.config_seed(2)), threads)
-    return {"value": round(CPU_SAMPLE / dt / 1e6, 4), "unit": "Mpts/s", "cores": threads, "kind": "port",
-            "sample": cpu_sample_desc(threads)}
+    dt = cpu_build(pts, threads)
+    return {"value": round(len(pts) / dt / 1e6, 4), "unit": "Mpts/s", "cores": threads, "kind": "port",
+            "seconds": round(dt, 2), "sample": cpu_sample_desc(threads, len(pts))}
 
 
 def run_reference(args, rank):
+    """The reference arm: the CPU restatement of the reference's parallel path
+    on the same 1M-point workload as the GPU arm (warm-up on a 20k sample)."""
     if rank != 0:
         return
     from voronoids_gb300 import workloads as W
     threads = cpu_threads()
-    p = W.uniform_points(CPU_SAMPLE, 3, W.config_seed(2))
+    p = W.c2_points() if args.n == N_POINTS else W.uniform_points(args.n, 3, W.config_seed(2))
     for _ in range(args.warmup):
         cpu_build(p[:20_000], threads)
     times = [cpu_build(p, threads) for _ in range(args.steps)]
     ms = 1e3 * float(np.mean(times))
-    v = CPU_SAMPLE / (ms / 1e3) / 1e6
+    v = len(p) / (ms / 1e3) / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mpts/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"uniform 3D points in [0,1)^3, seeded; bounded CPU sample of {CPU_SAMPLE} "
-                               f"(the GPU arm triangulates {args.n})", "points": CPU_SAMPLE},
+        "config": {"workload": "1M points i.i.d. uniform in [0,1)^3 (splitmix64 seed 0xD1A00002), exact 3D "
+                               "Delaunay tetrahedralization, sorted input-index edge list (the GPU arm's workload); "
+                               "warm-up steps on its first 20,000 points", "points": len(p)},
         "cpu_baseline": {"value": round(v, 4), "unit": "Mpts/s", "cores": threads, "kind": "port",
-                         "sample": cpu_sample_desc(threads)},
+                         "sample": cpu_sample_desc(threads, len(p))},
         "e2e": {"value": round(v, 4), "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def run_c3(args):
-    """Near-degenerate 3D build (jittered lattice + tight Gaussian clusters):
-    time, exactness and the share of predicates each precision tier decided."""
+def golden_digest(name):
+    """(rows, sha256) of the oracle's edge list of a workload (tests/golden/big_edges.json)."""
+    with open(os.path.join(ROOT, "tests", "golden", "big_edges.json")) as f:
+        g = json.load(f)[name]
+    return g["edges"], g["sha256"]
+
+
+def edge_digest(uv_dev, m):
+    """(rows, sha256) of the first m device uint32 edge pairs as little-endian int64."""
+    import hashlib
+    e = uv_dev[:m].cpu().numpy().astype("<i8")
+    return int(e.shape[0]), hashlib.sha256(np.ascontiguousarray(e).tobytes()).hexdigest()
+
+
+def timed_builds(L, tree, pts_d, n, uv_d, cap, steps, warmup, flush, stream):
+    """CUDA-event milliseconds of `steps` builds (vd_delaunay_device), L2 flushed before each."""
     import torch
-    from voronoids_gb300 import _native
-    from voronoids_gb300 import workloads as W
-    L = _native.load()
-    pts_h = W.c3_points()
-    n = len(pts_h)
-    pts_d = torch.from_numpy(pts_h).cuda()
-    cap = 10 * n + 1024
-    uv_d = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    stream = torch.cuda.current_stream()
-    st = ctypes.c_int(0)
-    tree = ctypes.c_void_p(L.vd_tree_new_device(3, ctypes.c_void_p(pts_d.data_ptr()), n,
-                                                ctypes.c_void_p(stream.cuda_stream), ctypes.byref(st)))
     m = ctypes.c_int64(0)
 
     def step():
@@ -220,12 +223,10 @@ def run_c3(args):
         if rc not in (0, 4):
             raise SystemExit(f"vd_delaunay_device failed: {rc}")
 
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(warmup):
         step()
     times = []
-    clk = Clocks(0)
-    clk.start()
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.fill_(1)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -234,7 +235,62 @@ def run_c3(args):
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1))
-    clocks = clk.stop()
+    return times, int(m.value)
+
+
+def measure_c1(L, steps, flush):
+    """C1: 10,000 uniform 2D points.  GPU build (device-resident, events),
+    parity with the oracle's digest, and the reference's own path for this
+    size -- sequential insert_point calls (src/lib.rs:117-121), restated with
+    its float conflict test on one host thread."""
+    import torch
+    from voronoids_gb300 import workloads as W
+    pts_h = W.c1_points()
+    n = len(pts_h)
+    pts_d = torch.from_numpy(pts_h).cuda()
+    cap = 4 * n + 1024
+    uv_d = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    st = ctypes.c_int(0)
+    tree = ctypes.c_void_p(L.vd_tree_new_device(2, ctypes.c_void_p(pts_d.data_ptr()), n,
+                                                ctypes.c_void_p(stream.cuda_stream), ctypes.byref(st)))
+    times, m = timed_builds(L, tree, pts_d, n, uv_d, cap, steps, 3, flush, stream)
+    L.vd_tree_free(tree)
+    rows, sha = edge_digest(uv_d, m)
+    ms = float(np.mean(times))
+    from oracle import oracle as O
+    cpu = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        f = O.FloatTriangulation(pts_h)
+        _ = f.edges()
+        cpu.append(time.perf_counter() - t0)
+    cpu_s = float(np.median(cpu))
+    return {"points": n, "value": round(n / (ms / 1e3) / 1e6, 4), "unit": "Mpts/s", "ms_per_step": round(ms, 3),
+            "edges": m, "parity_oracle_digest": (rows, sha) == golden_digest("c1"),
+            "cpu_baseline": {"value": round(n / cpu_s / 1e6, 4), "unit": "Mpts/s", "cores": 1, "kind": "port",
+                             "sample": "the full 10,000 points per run, median of 5: the reference's sequential "
+                                       "path (new + insert_point per point, src/lib.rs:117-121 and "
+                                       "src/delaunay_tree.rs:33-211) restated in C++ with its f64 circumsphere "
+                                       "and strict in_sphere test (oracle/ FloatTriangulation)"}}
+
+
+def measure_c3(L, steps, warmup, flush):
+    """C3: 262,144 near-degenerate 3D points: time, per-stage fallback rates of
+    the predicate tiers, the validator and the oracle's digest."""
+    import torch
+    from voronoids_gb300 import _native
+    from voronoids_gb300 import workloads as W
+    pts_h = W.c3_points()
+    n = len(pts_h)
+    pts_d = torch.from_numpy(pts_h).cuda()
+    cap = 10 * n + 1024
+    uv_d = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    st = ctypes.c_int(0)
+    tree = ctypes.c_void_p(L.vd_tree_new_device(3, ctypes.c_void_p(pts_d.data_ptr()), n,
+                                                ctypes.c_void_p(stream.cuda_stream), ctypes.byref(st)))
+    times, m = timed_builds(L, tree, pts_d, n, uv_d, cap, steps, warmup, flush, stream)
     s1 = _native.VdStats()
     L.vd_get_stats(tree, ctypes.byref(s1))
     stats = {k: getattr(s1, k) for k, _ in s1._fields_}
@@ -242,56 +298,78 @@ def run_c3(args):
     viol = np.zeros(6, dtype=np.int64)
     L.vd_check_delaunay(tree, ctypes.byref(ok), viol.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
     L.vd_tree_free(tree)
+    rows, sha = edge_digest(uv_d, m)
     tot = stats["pred_f32"] + stats["pred_f64"] + stats["pred_exact"]
     ms = float(np.mean(times))
-    line = {
-        "metric": "Mpts/s 3D near-degenerate build; predicate tier shares", "value": round(n / (ms / 1e3) / 1e6, 4),
-        "unit": "Mpts/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "262,144 3D points: 131,072 distinct sites of the 64^3 lattice (i/64) with uniform "
-                               "jitter +-1e-12 per coordinate, 131,072 from 64 Gaussians (centres uniform in the "
-                               "cube, sigma 0.01, not clipped); splitmix64 seed 0xD1A00003", "points": n,
-                   "l2": "flushed between steps (256 MB write)"},
+    return {
+        "points": n, "value": round(n / (ms / 1e3) / 1e6, 4), "unit": "Mpts/s", "ms_per_step": round(ms, 3),
+        "steps": steps,
         "predicates": {"decided_f32_filter": stats["pred_f32"], "decided_f64_filter": stats["pred_f64"],
                        "decided_exact": stats["pred_exact"], "of_exact_by_perturbation": stats["pred_sos"],
                        "fallback_rate_f32_to_f64": round((stats["pred_f64"] + stats["pred_exact"]) / max(tot, 1), 6),
                        "fallback_rate_f64_to_exact": round(stats["pred_exact"] /
                                                            max(stats["pred_f64"] + stats["pred_exact"], 1), 6)},
-        "validator_ok": bool(ok.value), "violations": viol.tolist(), "edges": int(m.value),
+        "validator_ok": bool(ok.value), "violations": viol.tolist(), "edges": m,
+        "parity_oracle_digest": (rows, sha) == golden_digest("c3"),
         "build_stats": {k: stats[k] for k in ("rounds", "max_cavity", "max_facets", "spilled", "cavity_tests")},
+    }
+
+
+def run_c3(args):
+    """Near-degenerate 3D build (jittered lattice + tight Gaussian clusters):
+    time, exactness and the share of predicates each precision tier decided."""
+    import torch
+    from voronoids_gb300 import _native
+    L = _native.load()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    clk = Clocks(0)
+    clk.start()
+    r = measure_c3(L, args.steps, max(args.warmup, 3), flush)
+    clocks = clk.stop()
+    line = {
+        "metric": "Mpts/s 3D near-degenerate build; predicate tier shares", "value": r["value"],
+        "unit": "Mpts/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": C3_DESC, "points": r["points"], "l2": "flushed between steps (256 MB write)"},
+        "predicates": r["predicates"], "validator_ok": r["validator_ok"], "violations": r["violations"],
+        "edges": r["edges"], "parity_oracle_digest": r["parity_oracle_digest"], "build_stats": r["build_stats"],
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
 
 
-def run_c4(args):
-    """4,096 independent 3D sets (log-uniform 32..65,536 points): one batched
-    build per step against one build per set, same GPU, same outputs."""
+C3_DESC = ("262,144 3D points: 131,072 distinct sites of the 64^3 lattice (i/64) with uniform jitter +-1e-12 per "
+           "coordinate, 131,072 from 64 Gaussians (centres uniform in the cube, sigma 0.01, not clipped); "
+           "splitmix64 seed 0xD1A00003")
+
+
+def measure_c4(L, nsets, steps, warmup, flush, autotune):
+    """`nsets` independent 3D sets (log-uniform 32..65,536 points): one batched
+    build per step against one build per set on the same GPU, set by set equal."""
     import torch
-    from voronoids_gb300 import _native
     from voronoids_gb300 import workloads as W
-    L = _native.load()
-    pts_h, off = W.c4_sets()
-    n, nsets = int(off[-1]), len(off) - 1
+    pts_h, off = W.c4_sets(nsets)
+    n = int(off[-1])
     pts_d = torch.from_numpy(pts_h).cuda()
     cap = 9 * n
     uv_d = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
     st = ctypes.c_int(0)
     tree = ctypes.c_void_p(L.vd_tree_create(3, ctypes.c_void_p(stream.cuda_stream), ctypes.byref(st)))
     eoff = np.zeros(nsets + 1, dtype=np.int64)
     i64p = ctypes.POINTER(ctypes.c_int64)
     offp = off.astype(np.int64)
-
-    # autotune launch shape and round settings on a 2M-point sample of the sets
-    tuned = np.zeros(9, dtype=np.int64)
-    rc = L.vd_autotune_batch(tree, ctypes.c_void_p(pts_d.data_ptr()), offp.ctypes.data_as(i64p), nsets, 2_000_000,
-                             tuned.ctypes.data_as(i64p))
-    if rc not in (0, 4):
-        raise SystemExit(f"vd_autotune_batch failed: {rc}")
-    tuned = dict(zip(("warps_per_sm", "blocks_per_sm", "passes", "thin", "ratio_x1000", "sample_us",
-                      "sample_points", "sample_sets", "adjacent"), tuned.tolist()))
+    tuned = None
+    if autotune:
+        # launch shape and round settings tuned on a 2M-point sample of the sets
+        tv = np.zeros(9, dtype=np.int64)
+        rc = L.vd_autotune_batch(tree, ctypes.c_void_p(pts_d.data_ptr()), offp.ctypes.data_as(i64p), nsets,
+                                 2_000_000, tv.ctypes.data_as(i64p))
+        if rc not in (0, 4):
+            raise SystemExit(f"vd_autotune_batch failed: {rc}")
+        tuned = dict(zip(("warps_per_sm", "blocks_per_sm", "passes", "thin", "ratio_x1000", "sample_us",
+                          "sample_points", "sample_sets", "adjacent"), tv.tolist()))
 
     def batched():
         rc = L.vd_batch_delaunay_device(tree, ctypes.c_void_p(pts_d.data_ptr()), offp.ctypes.data_as(i64p), nsets,
@@ -299,13 +377,11 @@ def run_c4(args):
         if rc not in (0, 4):
             raise SystemExit(f"vd_batch_delaunay_device failed: {rc}")
 
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(warmup):
         batched()
-    clk = Clocks(0)
-    clk.start()
     times = []
     launches0 = L.vd_kernel_launches()
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.fill_(1)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -314,22 +390,10 @@ def run_c4(args):
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1))
-    launches = (L.vd_kernel_launches() - launches0) // max(args.steps, 1)
-    clocks = clk.stop()
+    launches = (L.vd_kernel_launches() - launches0) // max(steps, 1)
     ok = ctypes.c_int(0)
     L.vd_check_delaunay(tree, ctypes.byref(ok), None)
     ms = float(np.mean(times))
-    # end to end: host points in, host edges out (vd_batch_delaunay)
-    pts_pin = torch.from_numpy(pts_h).pin_memory()
-    uv_pin = torch.empty((cap, 2), dtype=torch.int32).pin_memory()
-    hp = ctypes.cast(ctypes.c_void_p(pts_pin.data_ptr()), ctypes.POINTER(ctypes.c_double))
-    etimes = []
-    for _ in range(max(1, args.steps // 2)):
-        t0 = time.perf_counter()
-        rc = L.vd_batch_delaunay(tree, hp, offp.ctypes.data_as(i64p), nsets, SEED,
-                                 ctypes.c_void_p(uv_pin.data_ptr()), cap, eoff.ctypes.data_as(i64p))
-        etimes.append(time.perf_counter() - t0)
-    ems = 1e3 * float(np.mean(etimes))
     ref_edges = uv_d[: int(eoff[-1])].clone()
     ref_eoff = eoff.copy()
     # one set per launch on a second tree, compared set by set
@@ -340,8 +404,8 @@ def run_c4(args):
                          out2.shape[0], ctypes.byref(m))
     mismatch = 0
     one_ms = 0.0
-    for s in range(nsets):
-        a, b = int(off[s]), int(off[s + 1])
+    for k in range(nsets):
+        a, b = int(off[k]), int(off[k + 1])
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -350,24 +414,96 @@ def run_c4(args):
         e1.record(stream)
         e1.synchronize()
         one_ms += e0.elapsed_time(e1)
-        if rc not in (0, 4) or m.value != ref_eoff[s + 1] - ref_eoff[s] or \
-                not torch.equal(out2[: m.value], ref_edges[ref_eoff[s]:ref_eoff[s + 1]]):
+        if rc not in (0, 4) or m.value != ref_eoff[k + 1] - ref_eoff[k] or \
+                not torch.equal(out2[: m.value], ref_edges[ref_eoff[k]:ref_eoff[k + 1]]):
             mismatch += 1
     L.vd_tree_free(t2)
+    return {"tree": tree, "points": n, "sets": nsets, "offsets": offp, "pts_h": pts_h, "cap": cap,
+            "value": round(n / (ms / 1e3) / 1e6, 4), "unit": "Mpts/s", "ms_per_step": round(ms, 3),
+            "one_set_per_launch": {"value": round(n / (one_ms / 1e3) / 1e6, 4), "unit": "Mpts/s",
+                                   "ms_total": round(one_ms, 1), "mismatching_sets": mismatch},
+            "batched_over_one_set_per_launch": round(one_ms / ms, 2), "autotuned": tuned,
+            "validator_ok": bool(ok.value), "edges": int(ref_eoff[-1]), "gpu_launches": int(launches)}
+
+
+def measure_reference_pattern(L, n_seq=CPU_PREFIX):
+    """voronoids.delaunay's own call pattern on the 1M-point workload
+    (src/lib.rs:104-125): new, then the first 1e5 points one insert_point
+    call each (vd_insert_point: one single-warp launch per point), then
+    add_points_to_tree for the rest (vd_insert_points), then the edge list.
+    Wall clock from host points to host edges; the edges must equal the
+    oracle's digest."""
+    from voronoids_gb300 import workloads as W
+    import torch
+    pts = W.c2_points()
+    n = len(pts)
+    st = ctypes.c_int(0)
+    dp = ctypes.POINTER(ctypes.c_double)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tree = ctypes.c_void_p(L.vd_tree_new(3, pts.ctypes.data_as(dp), n, ctypes.byref(st)))
+    base = pts.ctypes.data
+    for i in range(n_seq):
+        rc = L.vd_insert_point(tree, ctypes.cast(ctypes.c_void_p(base + 24 * i), dp))
+        if rc != 0:
+            raise SystemExit(f"vd_insert_point failed: {rc}")
+    t1 = time.perf_counter()
+    rest = np.ascontiguousarray(pts[n_seq:])
+    rc = L.vd_insert_points(tree, rest.ctypes.data_as(dp), n - n_seq, SEED)
+    if rc != 0:
+        raise SystemExit(f"vd_insert_points failed: {rc}")
+    m = ctypes.c_int64(0)
+    L.vd_num_edges(tree, ctypes.byref(m))
+    uv = np.zeros((m.value, 2), dtype=np.int64)
+    L.vd_edges(tree, uv.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), m.value, ctypes.byref(m))
+    t2 = time.perf_counter()
+    L.vd_tree_free(tree)
+    import hashlib
+    digest = (int(uv.shape[0]), hashlib.sha256(np.ascontiguousarray(uv, dtype="<i8").tobytes()).hexdigest())
+    return {"points": n, "sequential_points": n_seq, "sequential_s": round(t1 - t0, 3),
+            "us_per_insert_point": round(1e6 * (t1 - t0) / n_seq, 2), "rest_s": round(t2 - t1, 3),
+            "total_s": round(t2 - t0, 3), "value": round(n / (t2 - t0) / 1e6, 4), "unit": "Mpts/s",
+            "parity_oracle_digest": digest == golden_digest("c2")}
+
+
+def run_c4(args):
+    """4,096 independent 3D sets (log-uniform 32..65,536 points): one batched
+    build per step against one build per set, same GPU, same outputs."""
+    import torch
+    from voronoids_gb300 import _native
+    L = _native.load()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    clk = Clocks(0)
+    clk.start()
+    r = measure_c4(L, 4096, args.steps, max(args.warmup, 3), flush, autotune=True)
+    clocks = clk.stop()
+    tree, n, nsets, offp, cap = r["tree"], r["points"], r["sets"], r["offsets"], r["cap"]
+    # end to end: host points in, host edges out (vd_batch_delaunay)
+    pts_pin = torch.from_numpy(r["pts_h"]).pin_memory()
+    uv_pin = torch.empty((cap, 2), dtype=torch.int32).pin_memory()
+    hp = ctypes.cast(ctypes.c_void_p(pts_pin.data_ptr()), ctypes.POINTER(ctypes.c_double))
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    eoff = np.zeros(nsets + 1, dtype=np.int64)
+    etimes = []
+    for _ in range(max(1, args.steps // 2)):
+        t0 = time.perf_counter()
+        L.vd_batch_delaunay(tree, hp, offp.ctypes.data_as(i64p), nsets, SEED, ctypes.c_void_p(uv_pin.data_ptr()),
+                            cap, eoff.ctypes.data_as(i64p))
+        etimes.append(time.perf_counter() - t0)
+    ems = 1e3 * float(np.mean(etimes))
     L.vd_tree_free(tree)
     line = {
-        "metric": "Mpts/s batched build, 4,096 3D sets", "value": round(n / (ms / 1e3) / 1e6, 4), "unit": "Mpts/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 3),
+        "metric": "Mpts/s batched build, 4,096 3D sets", "value": r["value"], "unit": "Mpts/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": r["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "4,096 independent 3D sets, sizes floor(exp(U(ln 32, ln 65536))), uniform [0,1)^3 "
                                "(splitmix64 seed 0xD1A00004), one batched build per step", "points": n,
                    "sets": nsets, "l2": "flushed between steps (256 MB write)"},
-        "one_set_per_launch": {"value": round(n / (one_ms / 1e3) / 1e6, 4), "unit": "Mpts/s",
-                               "ms_total": round(one_ms, 1), "mismatching_sets": mismatch},
-        "batched_over_one_set_per_launch": round(one_ms / ms, 2), "autotuned": tuned,
-        "validator_ok": bool(ok.value), "edges": int(ref_eoff[-1]), "clocks": clocks, "gpu_launches": int(launches),
+        "one_set_per_launch": r["one_set_per_launch"],
+        "batched_over_one_set_per_launch": r["batched_over_one_set_per_launch"], "autotuned": r["autotuned"],
+        "validator_ok": r["validator_ok"], "edges": r["edges"], "clocks": clocks, "gpu_launches": r["gpu_launches"],
         "e2e": {"value": round(n / (ems / 1e3) / 1e6, 4), "unit": "Mpts/s", "h2d_bytes_per_step": int(n * 24),
-                "d2h_bytes_per_step": int(ref_eoff[-1] * 8), "ms_per_step": round(ems, 3)},
+                "d2h_bytes_per_step": int(eoff[-1] * 8), "ms_per_step": round(ems, 3)},
     }
     print(json.dumps(line), flush=True)
 
@@ -634,9 +770,23 @@ def main():
     peak_b, _ = measured_peaks()
     build_roof = {"bytes_per_point": round(bpp, 1), "achieved": round(bpp * n / (ms / 1e3) / 1e9, 2),
                   "peak": peak_b, "unit": "GB/s", "frac": round(bpp * n / (ms / 1e3) / 1e9 / peak_b, 5)}
-    cpu = cpu_baseline() if rank == 0 and world == 1 else None
     edges = int(m.value)
     L.vd_tree_free(tree)
+    # the other configurations, measured beside the headline on rank 0:
+    # C1 (2D 10k), C3 (near-degenerate 262k), a 256-set sample of C4
+    subs = {}
+    if rank == 0 and world == 1 and not args.no_subs:
+        subs["c1"] = measure_c1(L, args.steps, flush)
+        subs["c3"] = measure_c3(L, min(args.steps, 5), 2, flush)
+        c4 = measure_c4(L, 256, min(args.steps, 5), 2, flush, autotune=False)
+        L.vd_tree_free(c4["tree"])
+        for k in ("tree", "offsets", "pts_h", "cap"):
+            c4.pop(k)
+        c4["workload"] = ("256 independent 3D sets, sizes floor(exp(U(ln 32, ln 65536))), uniform [0,1)^3 "
+                          "(splitmix64 seed 0xD1A00004, the C4 distribution), default tuning")
+        subs["c4_sample"] = c4
+        subs["reference_call_pattern"] = measure_reference_pattern(L)
+    cpu = cpu_baseline(pts_h) if rank == 0 and world == 1 else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": "Mpts/s", "n_gpus": world, "steps": args.steps,
@@ -657,6 +807,7 @@ def main():
             "build_roofline": build_roof,
             "ms_per_step_profiled": round(float(np.mean(ptimes)), 3),
         }
+        line.update(subs)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

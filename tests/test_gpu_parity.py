@@ -141,6 +141,14 @@ def test_insert_point_one_by_one_3d(vd, oracle):
     assert t.num_vertices == len(p)
     assert np.array_equal(t.edges(), oracle.Triangulation(p).edges())
     assert t.check_delaunay()
+    # a repeated point is skipped and recorded; points outside the super simplex are errors
+    with pytest.warns(RuntimeWarning):
+        t.insert_point(p[5])
+    assert np.array_equal(t.duplicates(), [[300, 5]])
+    assert np.array_equal(t.edges(), oracle.Triangulation(p).edges())
+    with pytest.raises(vd.VDError) as ei:
+        t.insert_point(np.array([50.0, 50.0, 50.0]))
+    assert ei.value.status == 6
     # then the rest of a larger set through add_points_to_tree, as the reference does past 1e5 points
     q = W.uniform_points(5000, 3, 20)
     t2 = vd.DelaunayTree(q)

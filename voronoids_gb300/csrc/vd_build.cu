@@ -1764,6 +1764,194 @@ __global__ void __launch_bounds__(128) k_rounds_small(DevTree T, Tuning tu, unsi
   }
 }
 
+// ---------------------------------------------------------------------------
+// One point, one warp: TreeUpdate::new + insert_point (src/delaunay_tree.rs:
+// 709-740, :125-211), the reference's sequential path (src/lib.rs:108-114),
+// without the round machinery.  The warp checks and stores the point, walks
+// to the simplex that contains it, searches the conflict region in shared
+// memory, writes the star into the removed slots (then fresh ones) and links
+// it, all in one launch.  No other insertion runs at the same time, so no
+// claims are needed, and no point is waiting to be relocated.  The outcome
+// goes to ctr->single: 0 inserted, E_DUPLICATE (skipped and recorded),
+// another error code, or -1 when the region outgrew the warp's shared memory
+// and nothing but the point record was written (the caller then inserts it
+// through the rounds).
+template <int D>
+__global__ void __launch_bounds__(32) k_insert_one(DevTree T, double x, double y, double z, int vid) {
+  constexpr int NV = D + 1;
+  constexpr int MAXC = Cap<D>::MAXC, MAXF = Cap<D>::MAXF, HS = Cap<D>::HS;
+  constexpr int HR = WarpCommit<D>::HR;
+  __shared__ WarpCav<D> C;
+  __shared__ WarpCommit<D> W;
+  __shared__ __align__(16) int F[6 * MAXF];
+  __shared__ int s_start, s_status;
+  const int lane = threadIdx.x;
+  Counters* ctr = T.ctr;
+  vdp::Tally tl = {0, 0, 0, 0};
+  int perr = 0;
+  const double c[3] = {x, y, D == 3 ? z : 0.0};
+  const vdp::FPt fq = vdp::split_point(c[0], c[1], c[2]);
+  if (lane == 0) {
+    s_status = 0;
+    s_start = -1;
+    const double lo = 7.006492321624085e-46;  // 2^-150
+    const double hi = 1.4272476927059599e45;  // 2^150
+    for (int k = 0; k < 3; ++k) {
+      const double a = fabs(c[k]);
+      if (!(a <= 1.7976931348623157e308)) s_status = E_NONFINITE;
+      else if (s_status == 0 && a != 0.0 && (a < lo || a > hi)) s_status = E_RANGE;
+    }
+    if (s_status == 0 && bad_vert(T, vid)) s_status = E_INTERNAL;
+    if (s_status == 0) {
+      reinterpret_cast<double4_32a*>(T.pts)[vid] = make_double4_32a(c[0], c[1], c[2], 0.0);
+      T.ptf[vid] = fq;
+      const SetGeo& g = T.sets[0];
+      vdp::VPt sv[NV];
+      for (int j = 0; j < NV; ++j) sv[j] = load_pt(T, g.sup[j]);
+      const vdp::VPt p{c[0], c[1], c[2], 0.0};
+      if (vdp::exit_face<D, true>(sv, p, (1u << NV) - 1, tl, perr) >= 0) s_status = E_OUTSIDE;
+    }
+    if (s_status == 0) {
+      // walk from the finest hint of the point's cell (as k_activate)
+      const SetGeo& g = T.sets[0];
+      int ic[3];
+      hint_cell<D>(g, fq, ic);
+      int cur = -1;
+      for (int l = g.hint_levels; l >= 0 && cur < 0; --l) cur = T.hint[hint_at<D>(g, ic, l)];
+      if (cur < 0) cur = g.root;
+      int4 v, nn;
+      load_simplex(T, cur, v, nn);
+      for (int k = 0; k < 64 && v.x < 0; ++k) {  // dead slot: into the star that replaced it
+        cur = nn.x >> 2;
+        if (nn.x < 0 || bad_simp(T, cur)) {
+          s_status = E_INTERNAL;
+          break;
+        }
+        load_simplex(T, cur, v, nn);
+      }
+      int step = 0;
+      const int cap = 1 << 16;
+      for (; s_status == 0 && step < cap; ++step) {
+        vdp::FPt fv[NV];
+        for (int j = 0; j < NV; ++j) fv[j] = load_fpt(T, get4(v, j));
+        auto load64 = [&](vdp::VPt* v64, vdp::VPt& p64) {
+          for (int j = 0; j < NV; ++j) v64[j] = load_pt(T, get4(v, j));
+          p64 = vdp::VPt{c[0], c[1], c[2], 0.0};
+        };
+        const int f = vdp::exit_face_hl<D>(fv, fq, (1u << NV) - 1, tl, perr, load64);
+        if (f < 0) break;
+        const int code = get4(nn, f);
+        if (code < 0 || bad_simp(T, code >> 2)) {
+          s_status = code < 0 ? E_OUTSIDE : E_INTERNAL;
+          break;
+        }
+        cur = code >> 2;
+        load_simplex(T, cur, v, nn);
+      }
+      if (step == cap) s_status = E_WALK;
+      if (s_status == 0) {
+        // a duplicate of a vertex of its simplex is skipped and recorded
+        const vdp::VPt q{c[0], c[1], c[2], 0.0};
+        int dup = -1;
+        for (int j = 0; j < NV; ++j) {
+          const int w = get4(v, j);
+          if (same_point_bits(load_pt(T, w), q)) dup = w;
+        }
+        if (dup >= 0) {
+          const int k = atomicAdd(&ctr->ndup, 1);
+          if (k < T.cap_dups) T.dups[k] = make_int2(vid, dup);
+          s_status = E_DUPLICATE;
+        }
+      }
+      s_start = cur;
+    }
+    if (s_status != 0 && s_status != E_DUPLICATE) set_error(ctr, s_status);
+  }
+  __syncwarp();
+  if (s_status != 0) {
+    if (lane == 0) ctr->single = s_status;
+    return;
+  }
+  const int start = s_start;
+  int4 v0, n0;
+  load_simplex(T, start, v0, n0);
+  unsigned long long ntests = 0;
+  const CavStore S{C.cav, C.cv, C.cn, C.hkey, C.fr, MAXC, MAXF, HS};
+  cavity_search<D, 0>(T, S, C.ctl, lane, start, v0, n0, vid, fq, tl, perr, ntests);
+  if (C.ctl.flags) {  // too large for the warp: the rounds insert it
+    if (lane == 0) ctr->single = -1;
+    return;
+  }
+  const int ncav = C.ctl.ncav, nfac = C.ctl.nfac;
+  expand_facets(C.fr, C.cv, nfac, vid, F, lane);
+  for (int i = lane; i < HR; i += 32) {
+    W.rk[i] = ~0ull;
+    W.ra[i] = -1;
+  }
+  for (int i = lane; i < ncav; i += 32) W.first[i] = 0x7fffffff;
+  __syncwarp();
+  // slots: the first facet of cavity simplex k takes k's slot, the others
+  // the cavity slots left over, then fresh ones
+  for (int j = lane; j < nfac; j += 32) atomicMin(&W.first[F[6 * j + 5] >> 2], j);
+  __syncwarp();
+  int nfree = 0;
+  for (int i0 = 0; i0 < ncav; i0 += 32) {
+    const int i = i0 + lane;
+    const bool fr = i < ncav && W.first[i] == 0x7fffffff;
+    const unsigned m = __ballot_sync(FULL, fr);
+    if (fr) W.freeslot[nfree + __popc(m & ((1u << lane) - 1))] = C.cav[i];
+    nfree += __popc(m);
+  }
+  const int fresh = max(0, nfac - ncav);
+  int base = 0;
+  if (lane == 0 && fresh > 0) base = atomicAdd(&ctr->nsimp, fresh);
+  base = __shfl_sync(FULL, base, 0);
+  if (base + fresh > T.cap_simp) {  // the caller keeps spare slots: cannot happen
+    if (lane == 0) {
+      set_error(ctr, E_INTERNAL);
+      ctr->single = E_INTERNAL;
+    }
+    return;
+  }
+  int nsec = 0;
+  for (int j0 = 0; j0 < nfac; j0 += 32) {
+    const int j = j0 + lane;
+    int id = 0;
+    bool sec = false;
+    if (j < nfac) {
+      const int k = F[6 * j + 5] >> 2;
+      sec = W.first[k] != j;
+      if (!sec) id = C.cav[k];
+    }
+    const unsigned m = __ballot_sync(FULL, sec);
+    if (sec) {
+      const int t = nsec + __popc(m & ((1u << lane) - 1));
+      id = t < nfree ? W.freeslot[t] : base + (t - nfree);
+    }
+    if (j < nfac) W.id[j] = id;
+    nsec += __popc(m);
+  }
+  __syncwarp();
+  const int id0 = W.id[0];
+  for (int t = nsec + lane; t < nfree; t += 32)
+    store_simplex(T, W.freeslot[t], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
+  // no slot carries round -2 in `killed`, so every outer neighbour is repointed
+  write_star<D>(T, W, F, nfac, vid, -2, lane);
+  if (perr) set_error(ctr, E_PRECISION);
+  flush_tally(ctr, tl, ntests, 0);
+  if (lane == 0) {
+    write_hints<D>(T, vid, fq, id0);
+    ctr->ninserted += 1;
+    ctr->winners += 1;
+    ctr->created += nfac;
+    ctr->killed += ncav;
+    ctr->holes += max(0, ncav - nfac);
+    ctr->max_cav = max(ctr->max_cav, ncav);
+    ctr->max_fac = max(ctr->max_fac, nfac);
+    ctr->single = 0;
+  }
+}
+
 template <int D>
 constexpr size_t small_rounds_smem() {
   return 4 * sizeof(WarpCav<D>) > 4 * sizeof(WarpCommit<D>) ? 4 * sizeof(WarpCav<D>) : 4 * sizeof(WarpCommit<D>);
@@ -1946,6 +2134,14 @@ int launch_small_rounds(const DevTree& T, cudaStream_t stream, int dim, const Tu
   }
   note_launches(1);
   return E_OK;
+}
+
+void launch_insert_one(const DevTree& T, cudaStream_t stream, int dim, const double* c, int vid) {
+  note_launches(1);
+  if (dim == 3)
+    k_insert_one<3><<<1, 32, 0, stream>>>(T, c[0], c[1], c[2], vid);
+  else
+    k_insert_one<2><<<1, 32, 0, stream>>>(T, c[0], c[1], 0.0, vid);
 }
 
 void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, const Feed& fd, Prof* pf) {

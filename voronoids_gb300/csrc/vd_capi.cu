@@ -1245,7 +1245,31 @@ int vd_insert_points(vd_tree* t, const double* pts, int64_t n, uint64_t seed) {
   return rc;
 }
 
-int vd_insert_point(vd_tree* t, const double* p) { return vd_insert_points(t, p, 1, 0); }
+// One point: a single-warp kernel (k_insert_one) does the whole insertion in
+// one launch, the way the reference's insert_point applies one TreeUpdate;
+// only a conflict region too large for the warp's shared memory (or a batched
+// tree) goes through the insertion rounds instead.
+int vd_insert_point(vd_tree* t, const double* p) {
+  if (ready(t) || !p) return VD_ERR_ARG;
+  if (!t->has_geometry || t->nsets != 1) return vd_insert_points(t, p, 1, 0);
+  int rc = ensure_points(t, 1);
+  if (rc) return rc;
+  rc = ensure_simplices(t, (int64_t)t->hctr->nsimp + 4096);  // above any star a warp can write
+  if (rc) return rc;
+  const double c[3] = {p[0], p[1], t->dim == 3 ? p[2] : 0.0};
+  t->edges_valid = false;
+  vd::launch_insert_one(t->T, t->stream, t->dim, c, (int)t->nverts);
+  rc = sync_counters(t);
+  if (rc) return rc;
+  const int out = t->hctr->single;
+  if (out == -1) return vd_insert_points(t, p, 1, 0);
+  if (out == VD_OK || out == VD_ERR_DUPLICATE) {
+    t->nverts += 1;
+    t->calls++;
+    t->inserted = t->hctr->ninserted;
+  }
+  return out;
+}
 
 int vd_num_vertices(vd_tree* t, int64_t* n) {
   if (ready(t) || !n) return VD_ERR_ARG;

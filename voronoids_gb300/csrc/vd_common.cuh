@@ -100,6 +100,7 @@ struct Counters {
   // grid barrier and loop decision of the small-round kernel
   unsigned bar_count, bar_gen;
   int bar_abort, coop_go;
+  int single;                       // outcome of the last one-point insertion (k_insert_one)
 };
 
 // Points of one insertion call are split into priority levels of
@@ -285,6 +286,10 @@ int prepare_round_kernels();
 // advanced by the round's first kernel), so a captured sequence of rounds
 // can be replayed.
 void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, const Feed& fd, Prof* pf);
+// One point inserted by a single warp (no rounds): its coordinates c[0..dim),
+// its vertex id vid (the next one of the tree).  ctr->single receives the
+// outcome (see k_insert_one in vd_build.cu).
+void launch_insert_one(const DevTree& T, cudaStream_t stream, int dim, const double* c, int vid);
 // Rounds while few points are active, in one cooperative launch (all blocks
 // resident, grid barrier between phases): runs until the next round's active
 // set reaches `max_active`, the call is done, `max_rounds` rounds ran, a pool
