@@ -139,6 +139,19 @@ int vd_simplices(vd_tree* t, int32_t* verts, int32_t* nbrs, int64_t cap, int64_t
  * centers: 3 doubles per simplex (z = 0 in 2D).  *n receives the count. */
 int vd_circumspheres(vd_tree* t, double* centers, double* radii, int64_t cap, int64_t* n);
 
+/* Voronoi dual (the reference's stated purpose, README.md:2-4; the reference
+ * keeps only the Voronoi vertices, Simplex::center / radius,
+ * src/delaunay_tree.rs:10-17).  Voronoi vertices: vd_circumspheres.
+ * Voronoi edges: one per interior facet, the (i, j) pair (i < j) of the two
+ * live simplices sharing it, numbered as vd_simplices exports them, sorted;
+ * pairs NULL to query the count (*n). */
+int vd_voronoi_edges(vd_tree* t, int64_t* pairs, int64_t cap, int64_t* n);
+/* Voronoi cells: the live simplices incident to input vertex v (the vertices
+ * of its cell, vd_simplices numbering) are ids[offsets[v] .. offsets[v+1]),
+ * sorted.  offsets: vd_num_vertices + 1 entries (always filled); ids NULL to
+ * query the sizes.  A skipped duplicate has an empty cell. */
+int vd_voronoi_cells(vd_tree* t, int64_t* offsets, int64_t* ids, int64_t cap);
+
 /* Sorted Delaunay edge list among inserted points. */
 int vd_num_edges(vd_tree* t, int64_t* n);
 int vd_edges(vd_tree* t, int64_t* uv, int64_t cap, int64_t* n);

@@ -35,6 +35,12 @@ def test_dictionary_view(vd, oracle, dim):
         assert np.allclose(d, s.radius, rtol=1e-9, atol=0), (sid, d, s.radius)
         for nb in s.neighbors:
             assert sid in simp[nb].neighbors
+    # and they agree with the reference's own formula (src/geometry.rs:2-56,
+    # restated by the oracle) within 1e-8 of the radius
+    for sid, s in list(simp.items())[::5]:
+        cr, rr = oracle.circumsphere_float(np.array([coords[v] for v in s.vertices]))
+        assert np.all(np.abs(np.array(s.center)[:dim] - cr[:dim]) <= 1e-8 * rr), sid
+        assert abs(s.radius - rr) <= 1e-8 * rr, sid
     # the edge graph of the view is the oracle's
     e = set()
     for s in simp.values():

@@ -29,7 +29,7 @@ EXPORTS = [
     "vd_batch_delaunay", "vd_batch_delaunay_device", "vd_num_sets", "vd_tree_create",
     "vd_set_launch", "vd_autotune_batch", "vd_locate_points", "vd_set_adjacent", "vd_circumspheres", "vd_set_small_rounds", "vd_set_early_phase", "vd_set_exact_tier",
     "vd_server_new", "vd_server_submit", "vd_server_poll", "vd_server_result", "vd_server_stats", "vd_server_free",
-    "vd_check_triangulation",
+    "vd_check_triangulation", "vd_voronoi_edges", "vd_voronoi_cells",
 ]
 
 
@@ -82,6 +82,8 @@ def load(path=LIB_PATH):
         "vd_edges_device": ([vp, vp, i64, i64p], ctypes.c_int),
         "vd_check_delaunay": ([vp, ip, i64p], ctypes.c_int),
         "vd_check_triangulation": ([ctypes.c_int, dp, i64, i32p, i32p, i64, ip, i64p], ctypes.c_int),
+        "vd_voronoi_edges": ([vp, i64p, i64, i64p], ctypes.c_int),
+        "vd_voronoi_cells": ([vp, i64p, i64p, i64], ctypes.c_int),
         "vd_duplicates": ([vp, i64p, i64, i64p], ctypes.c_int),
         "vd_get_stats": ([vp, ctypes.POINTER(VdStats)], ctypes.c_int),
         "vd_status_str": ([ctypes.c_int], ctypes.c_char_p),

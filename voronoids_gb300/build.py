@@ -22,7 +22,7 @@ LIB = os.path.join(HERE, "libvoronoids_gpu.so")
 HOSTLIB = os.path.join(HERE, "libvd_pred_host.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["vd_build.cu", "vd_edges.cu", "vd_check.cu", "vd_size.cu", "vd_locate.cu", "vd_noalloc.cu", "vd_capi.cu",
-           "vd_server.cu"]
+           "vd_server.cu", "vd_dual.cu"]
 HEADERS = ["vd_common.cuh", "vd_predicates.cuh"]
 
 

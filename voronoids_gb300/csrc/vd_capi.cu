@@ -1847,6 +1847,117 @@ int vd_circumspheres(vd_tree* t, double* centers, double* radii, int64_t cap, in
   return rc;
 }
 
+// Live ranks of the tree's slots (vd_simplices numbering): rank[s], and the
+// live count.  The caller frees flags, rank and tmp.
+int live_ranks(vd_tree* t, int** flags, int** rank, int** tmp, int* nsimp, int* live) {
+  *flags = *rank = *tmp = nullptr;
+  int rc = sync_counters(t);
+  if (rc) return rc;
+  *nsimp = t->hctr->nsimp;
+  if (dalloc(flags, *nsimp + 1) || dalloc(rank, *nsimp + 1) || dalloc(tmp, vd::scan_scratch_ints(*nsimp + 1)))
+    return VD_ERR_NOMEM;
+  vd::launch_live_rank(t->T, launch_of(t), *nsimp, *flags, *rank, *tmp);
+  cudaMemcpyAsync(t->h_pair, *rank + *nsimp, sizeof(int), cudaMemcpyDeviceToHost, t->stream);
+  rc = cuda_status(cudaStreamSynchronize(t->stream));
+  *live = t->h_pair[0];
+  return rc;
+}
+
+int vd_voronoi_edges(vd_tree* t, int64_t* pairs, int64_t cap, int64_t* n) {
+  if (ready(t) || !t->has_geometry || !n) return VD_ERR_ARG;
+  int *flags, *rank, *tmp, nsimp = 0, live = 0;
+  int rc = live_ranks(t, &flags, &rank, &tmp, &nsimp, &live);
+  int *cnt = nullptr, *off = nullptr, *tmp2 = nullptr;
+  int2* d_out = nullptr;
+  const vd::Launch L = launch_of(t);
+  if (!rc && (dalloc(&cnt, live + 1) || dalloc(&off, live + 1) || dalloc(&tmp2, vd::scan_scratch_ints(live + 1))))
+    rc = VD_ERR_NOMEM;
+  int total = 0;
+  if (!rc) {
+    vd::launch_dual_edges(t->T, L, t->dim, nsimp, rank, cnt, off, tmp2, live, nullptr, false);
+    cudaMemcpyAsync(t->h_pair, off + live, sizeof(int), cudaMemcpyDeviceToHost, t->stream);
+    rc = cuda_status(cudaStreamSynchronize(t->stream));
+    total = t->h_pair[0];
+    *n = total;
+  }
+  if (!rc && pairs) {
+    if (cap < total) {
+      rc = VD_ERR_ARG;
+    } else if (dalloc(&d_out, (size_t)total + 1)) {
+      rc = VD_ERR_NOMEM;
+    } else {
+      vd::launch_dual_edges(t->T, L, t->dim, nsimp, rank, cnt, off, tmp2, live, d_out, true);
+      std::vector<int2> h(total);
+      cudaMemcpyAsync(h.data(), d_out, sizeof(int2) * total, cudaMemcpyDeviceToHost, t->stream);
+      rc = cuda_status(cudaStreamSynchronize(t->stream));
+      for (int64_t i = 0; i < total && !rc; ++i) {
+        pairs[2 * i] = h[i].x;
+        pairs[2 * i + 1] = h[i].y;
+      }
+    }
+  }
+  dfree(d_out);
+  dfree(cnt);
+  dfree(off);
+  dfree(tmp2);
+  dfree(flags);
+  dfree(rank);
+  dfree(tmp);
+  if (!rc && t->hctr->err) rc = t->hctr->err;
+  return rc;
+}
+
+int vd_voronoi_cells(vd_tree* t, int64_t* offsets, int64_t* ids, int64_t cap) {
+  if (ready(t) || !t->has_geometry || !offsets) return VD_ERR_ARG;
+  int *flags, *rank, *tmp, nsimp = 0, live = 0;
+  int rc = live_ranks(t, &flags, &rank, &tmp, &nsimp, &live);
+  const int n_in = (int)(t->nverts - t->ns);
+  int *cnt = nullptr, *off = nullptr, *tmp2 = nullptr, *buf = nullptr, *ucnt = nullptr, *big = nullptr,
+      *nbig = nullptr;
+  const vd::Launch L = launch_of(t);
+  if (!rc && (dalloc(&cnt, n_in + 2) || dalloc(&off, n_in + 2) || dalloc(&tmp2, vd::scan_scratch_ints(n_in + 2))))
+    rc = VD_ERR_NOMEM;
+  int total = 0;
+  std::vector<int> hoff;
+  if (!rc) {
+    vd::launch_cell_count(t->T, L, t->dim, nsimp, n_in, cnt, off, tmp2);
+    hoff.resize(n_in + 1);
+    cudaMemcpyAsync(hoff.data(), off, sizeof(int) * (n_in + 1), cudaMemcpyDeviceToHost, t->stream);
+    rc = cuda_status(cudaStreamSynchronize(t->stream));
+    total = hoff[n_in];
+    for (int i = 0; i <= n_in; ++i) offsets[i] = hoff[i];
+  }
+  if (!rc && ids) {
+    if (cap < total) {
+      rc = VD_ERR_ARG;
+    } else if (dalloc(&buf, (size_t)total + 1) || dalloc(&ucnt, n_in + 1) || dalloc(&big, n_in + 1) ||
+               dalloc(&nbig, 1)) {
+      rc = VD_ERR_NOMEM;
+    } else {
+      vd::launch_cell_fill(t->T, L, t->dim, nsimp, n_in, rank, cnt, off, buf);
+      if (vd::sort_buckets(L, n_in, off, buf, ucnt, big, nbig, t->d_pair, t->h_pair) != 0) rc = VD_ERR_CUDA;
+      if (!rc) {
+        std::vector<int> h(total);
+        cudaMemcpyAsync(h.data(), buf, sizeof(int) * total, cudaMemcpyDeviceToHost, t->stream);
+        rc = cuda_status(cudaStreamSynchronize(t->stream));
+        for (int64_t i = 0; i < total && !rc; ++i) ids[i] = h[i];
+      }
+    }
+  }
+  dfree(buf);
+  dfree(ucnt);
+  dfree(big);
+  dfree(nbig);
+  dfree(cnt);
+  dfree(off);
+  dfree(tmp2);
+  dfree(flags);
+  dfree(rank);
+  dfree(tmp);
+  if (!rc && t->hctr->err) rc = t->hctr->err;
+  return rc;
+}
+
 int vd_locate(vd_tree* t, const double* p, int64_t* out, int64_t cap, int64_t* n) {
   if (!n) return VD_ERR_ARG;
   int64_t off[2] = {0, 0};

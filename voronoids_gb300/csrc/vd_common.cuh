@@ -350,6 +350,26 @@ void launch_localize(const Launch& L, uint2* uv, int64_t m, const int* set_of, c
 void launch_set_edge_offsets(const Launch& L, const int* uoff, const long long* off, int nsets,
                              long long* eoff);
 
+// Sort and de-duplicate every bucket buf[off[u] .. off[u+1]) (u < n) in
+// place (vd_edges.cu); ucnt[u] receives the unique count.  big (n ints) and
+// nbig (1 int) are device scratch, h_pair pinned host scratch.  Synchronises;
+// returns 0, or -1 on a CUDA error.  sort_big_buckets sorts the nbig long
+// buckets listed in big[] (the warp pass leaves them to it).
+int sort_buckets(const Launch& L, int n, const int* off, int* buf, int* ucnt, int* big, int* nbig, int* d_pair,
+                 int* h_pair);
+int sort_big_buckets(const Launch& L, int n, const int* off, int* buf, int* ucnt, const int* big, int nbig);
+// Voronoi dual (vd_dual.cu).  Edges: with fill = false, cnt[rank] = interior
+// facets each live slot owns and off = their exclusive scan over the nlive
+// ranks; with fill = true, out[off[rank] ..] = (rank, partner rank) pairs.
+void launch_dual_edges(const DevTree& T, const Launch& L, int dim, int nsimp, const int* rank, int* cnt, int* off,
+                       int* tmp, int nlive, int2* out, bool fill);
+// Cells: cnt (n_in + 1) = simplices incident to each input vertex, off = scan;
+// fill scatters the live ranks into buf by vertex (cnt returns to zero).
+void launch_cell_count(const DevTree& T, const Launch& L, int dim, int nsimp, int n_in, int* cnt, int* off,
+                       int* tmp);
+void launch_cell_fill(const DevTree& T, const Launch& L, int dim, int nsimp, int n_in, const int* rank, int* cnt,
+                      const int* off, int* buf);
+
 // Validator: out[0..5] = non-positive, asymmetric, not Delaunay (exact),
 // not perturbed-Delaunay, hull facets, facets checked.
 void launch_check(const DevTree& T, const Launch& L, int dim, int nsimp,

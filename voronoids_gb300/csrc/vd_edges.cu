@@ -316,11 +316,22 @@ int64_t run_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_i
   if (h_total_pair[1] == 0) return h_total_pair[0];
 
   // long buckets: sort them in padded scratch, then redo the placement
-  const int nbig = h_total_pair[1];
+  if (sort_big_buckets(L, n_in, S.off, S.buf, S.ucnt, S.big, h_total_pair[1]) != 0) return -1;
+  note_launches(1);
+  exclusive_scan(S.ucnt, S.uoff, n_in, S.scan_tmp, st);
+  k_edge_out<<<L.blocks, 256, 0, st>>>(n_in, S.off, S.buf, S.ucnt, S.uoff, d_out, cap_out);
+  cudaMemcpyAsync(h_total_pair, S.uoff + n_in, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+  return h_total_pair[0];
+}
+
+int sort_big_buckets(const Launch& L, int n, const int* off, int* buf, int* ucnt, const int* big, int nbig) {
+  if (nbig <= 0) return 0;
+  cudaStream_t st = L.stream;
   std::vector<int> hbig(nbig);
-  std::vector<int> hoff(n_in + 1);
-  cudaMemcpyAsync(hbig.data(), S.big, sizeof(int) * nbig, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(hoff.data(), S.off, sizeof(int) * (n_in + 1), cudaMemcpyDeviceToHost, st);
+  std::vector<int> hoff(n + 1);
+  cudaMemcpyAsync(hbig.data(), big, sizeof(int) * nbig, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hoff.data(), off, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
   std::vector<long long> soff(nbig + 1, 0);
   for (int i = 0; i < nbig; ++i) {
@@ -336,16 +347,23 @@ int64_t run_edges(const DevTree& T, const Launch& L, int dim, int nsimp, int n_i
     return -1;
   }
   cudaMemcpyAsync(dsoff, soff.data(), sizeof(long long) * (nbig + 1), cudaMemcpyHostToDevice, st);
-  k_edge_uniq_big<<<nbig, 1024, 0, st>>>(S.big, S.off, S.buf, S.ucnt, scratch, dsoff);
-  note_launches(2);
-  exclusive_scan(S.ucnt, S.uoff, n_in, S.scan_tmp, st);
-  k_edge_out<<<L.blocks, 256, 0, st>>>(n_in, S.off, S.buf, S.ucnt, S.uoff, d_out, cap_out);
-  cudaMemcpyAsync(h_total_pair, S.uoff + n_in, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaError_t e = cudaStreamSynchronize(st);
+  k_edge_uniq_big<<<nbig, 1024, 0, st>>>(big, off, buf, ucnt, scratch, dsoff);
+  note_launches(1);
+  const cudaError_t e = cudaStreamSynchronize(st);
   cudaFree(scratch);
   cudaFree(dsoff);
-  if (e != cudaSuccess) return -1;
-  return h_total_pair[0];
+  return e == cudaSuccess ? 0 : -1;
+}
+
+int sort_buckets(const Launch& L, int n, const int* off, int* buf, int* ucnt, int* big, int* nbig, int* d_pair,
+                 int* h_pair) {
+  cudaStream_t st = L.stream;
+  cudaMemsetAsync(nbig, 0, sizeof(int), st);
+  note_launches(1);
+  k_edge_uniq<<<L.blocks, 256, 0, st>>>(n, off, buf, ucnt, big, nbig);
+  cudaMemcpyAsync(h_pair, nbig, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+  return sort_big_buckets(L, n, off, buf, ucnt, big, h_pair[0]);
 }
 
 }  // namespace vd

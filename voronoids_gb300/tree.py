@@ -255,6 +255,40 @@ class DelaunayTree:
                               ctypes.byref(n)), "simplices")
         return v, nb
 
+    def circumspheres(self):
+        """Circumcentre (3 per simplex, z = 0 in 2D) and radius of every live
+        simplex, in :meth:`simplices` order: the Voronoi vertices."""
+        L = _native.load()
+        n = ctypes.c_int64(0)
+        _check(L.vd_circumspheres(self._h, None, None, 0, ctypes.byref(n)), "circumspheres")
+        c = np.zeros((n.value, 3))
+        r = np.zeros(n.value)
+        _check(L.vd_circumspheres(self._h, _dp(c), _dp(r), n.value, ctypes.byref(n)), "circumspheres")
+        return c, r
+
+    def voronoi_edges(self):
+        """(m, 2) int64 pairs (i, j), i < j, of simplices sharing a facet: the
+        Voronoi edges between circumcentres i and j, sorted."""
+        L = _native.load()
+        n = ctypes.c_int64(0)
+        _check(L.vd_voronoi_edges(self._h, None, 0, ctypes.byref(n)), "voronoi_edges")
+        out = np.zeros((n.value, 2), dtype=np.int64)
+        _check(L.vd_voronoi_edges(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), n.value,
+                                  ctypes.byref(n)), "voronoi_edges")
+        return out
+
+    def voronoi_cells(self):
+        """(offsets, ids): the sorted simplices incident to input vertex v (the
+        vertices of its Voronoi cell) are ids[offsets[v]:offsets[v+1]]."""
+        L = _native.load()
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        off = np.zeros(self.num_vertices + 1, dtype=np.int64)
+        _check(L.vd_voronoi_cells(self._h, off.ctypes.data_as(i64p), None, 0), "voronoi_cells")
+        ids = np.zeros(max(int(off[-1]), 1), dtype=np.int64)
+        _check(L.vd_voronoi_cells(self._h, off.ctypes.data_as(i64p), ids.ctypes.data_as(i64p), ids.shape[0]),
+               "voronoi_cells")
+        return off, ids[: int(off[-1])]
+
     def check_delaunay(self, details=False):
         ok = ctypes.c_int(0)
         viol = (ctypes.c_int64 * 6)()
