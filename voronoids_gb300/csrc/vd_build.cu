@@ -1957,6 +1957,10 @@ constexpr size_t small_rounds_smem() {
   return 4 * sizeof(WarpCav<D>) > 4 * sizeof(WarpCommit<D>) ? 4 * sizeof(WarpCav<D>) : 4 * sizeof(WarpCommit<D>);
 }
 
+// Blocks of the small-round kernel (0: one per SM).
+#ifndef VD_SMALL_GRID
+#define VD_SMALL_GRID 0
+#endif
 // Resident blocks on the whole GPU of the strict-mode k_check (MODE 0) and
 // of the commit half (MODE 2), 2D and 3D.
 int g_check_wave[2] = {1 << 20, 1 << 20};
@@ -2102,8 +2106,10 @@ int prepare_once() {
     cudaGetLastError();
     s3 = s2 = 0;
   }
-  g_small_grid[1] = s3 > 0 ? sms : 0;
-  g_small_grid[0] = s2 > 0 ? sms : 0;
+  // a small grid keeps the grid barrier short (the rounds it runs are small)
+  const int cap3 = sms * s3, cap2 = sms * s2;
+  g_small_grid[1] = s3 > 0 ? (VD_SMALL_GRID > 0 ? std::min(VD_SMALL_GRID, cap3) : sms) : 0;
+  g_small_grid[0] = s2 > 0 ? (VD_SMALL_GRID > 0 ? std::min(VD_SMALL_GRID, cap2) : sms) : 0;
   return E_OK;
 }
 }  // namespace
