@@ -61,6 +61,10 @@ struct Cap;
 #define VD_CAP3_F 192
 #define VD_CAP3_H 256
 #endif
+// 1: k_cavity reads its next item's list entry and record one search ahead
+#ifndef VD_CAVITY_PIPE
+#define VD_CAVITY_PIPE 1
+#endif
 #ifndef VD_CAVITY_MIN_BLOCKS
 #define VD_CAVITY_MIN_BLOCKS 5
 #endif
@@ -900,12 +904,31 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
   const CavStore fast{W.cav, W.cv, W.cn, W.hkey, W.fr, MAXC, MAXF, HS};
   const int nw = nblk * 4;
   const int nsurv = T.ctr->nwl[0];
-  for (int it = bid * 4 + wib; it < nsurv; it += nw) {
-    const int c = T.wl[0][it];
-    const int4 cd = T.cand[c];
+  // the list entry and candidate record of the warp's next item are read one
+  // search ahead, so that a search starts with one round trip (its point and
+  // start simplex) instead of three
+  int it = bid * 4 + wib;
+  int c_next = it < nsurv ? T.wl[0][it] : 0;
+  int4 cd_next = it < nsurv ? T.cand[c_next] : make_int4(0, 0, 0, 0);
+  int c_after = it + nw < nsurv ? T.wl[0][it + nw] : 0;
+  for (; it < nsurv; it += nw) {
+    const int c = c_next;
+    const int4 cd = cd_next;
     const vdp::FPt fq = load_fpt(T, cd.x);
     int4 v0, n0;
     load_simplex(T, cd.y, v0, n0);
+#if VD_CAVITY_PIPE
+    if (it + nw < nsurv) {
+      c_next = c_after;
+      cd_next = T.cand[c_after];
+    }
+    if (it + 2 * nw < nsurv) c_after = T.wl[0][it + 2 * nw];
+#else
+    if (it + nw < nsurv) {
+      c_next = T.wl[0][it + nw];
+      cd_next = T.cand[c_next];
+    }
+#endif
     if (lane == 0) ++nsearched;
     const unsigned long long key = pe | (unsigned)cd.z;
     cavity_search<D, XT>(T, fast, W.ctl, lane, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
@@ -1050,14 +1073,15 @@ __device__ __forceinline__ void ridge_of(const int* r, int g, int qf, int& r0, i
 // neighbour that another winner of this round removed (adjacent mode) is left
 // alone: the two new simplices on that facet are linked at the start of
 // k_relocate (fix_body).
-__device__ __forceinline__ void emit_simplex(const DevTree& T, const int* r, int myid, int4 nn, int round) {
+__device__ __forceinline__ bool emit_simplex(const DevTree& T, const int* r, int myid, int4 nn, int round) {
   const int4 v = make_int4(r[0], r[1], r[2], r[3]);
   const int qf = r[5] & 3, o = r[4];
   store_simplex(T, myid, v, nn);
-  if (o >= 0 && !bad_simp(T, o >> 2) && T.killed[o >> 2].x != round) {
-    reinterpret_cast<int*>(T.simp + (o >> 2))[4 + (o & 3)] = (myid << 2) | qf;
-    T.touched[o >> 2] = round;
-  }
+  if (o < 0 || bad_simp(T, o >> 2)) return false;
+  if (T.killed[o >> 2].x == round) return true;  // another winner's cavity: linked by fix_body
+  reinterpret_cast<int*>(T.simp + (o >> 2))[4 + (o & 3)] = (myid << 2) | qf;
+  T.touched[o >> 2] = round;
+  return false;
 }
 
 // Star of one winner, small case.  The new simplices are written first, each
@@ -1071,18 +1095,21 @@ __device__ __forceinline__ void emit_simplex(const DevTree& T, const int* r, int
 __device__ __forceinline__ unsigned ridge_hash(int r0, int r1) {
   return ((unsigned)r0 * 0x9E3779B1u) ^ ((unsigned)r1 * 0x85EBCA77u);
 }
+// Returns, per lane, a bit for each of its facets (j = lane, lane + 32, ...)
+// whose outer neighbour another winner of this round removed.
 template <int D>
-__device__ void write_star(const DevTree& T, WarpCommit<D>& W, const int* __restrict__ FR, int nfac, int qv,
-                           int round, int lane) {
+__device__ unsigned write_star(const DevTree& T, WarpCommit<D>& W, const int* __restrict__ FR, int nfac, int qv,
+                               int round, int lane) {
   constexpr int NV = D + 1;
   constexpr int HR = WarpCommit<D>::HR;
   constexpr int LOG_HR = D == 3 ? 8 : 7;
   constexpr int PER_SWEEP = 2 * HR / 3;
   const unsigned long long EMPTY = ~0ull;
-  for (int j = lane; j < nfac; j += 32) {
+  unsigned dead = 0;
+  for (int j = lane, bit = 0; j < nfac; j += 32, ++bit) {
     const int* r = FR + 6 * j;
     const int qf = r[5] & 3;
-    emit_simplex(T, r, W.id[j], set4(make_int4(-1, -1, -1, -1), qf, r[4]), round);
+    if (emit_simplex(T, r, W.id[j], set4(make_int4(-1, -1, -1, -1), qf, r[4]), round)) dead |= 1u << bit;
   }
   const int sweeps = (nfac * D / 2 + PER_SWEEP - 1) / PER_SWEEP;
   // the table is empty on entry (cleared when the warp starts, and after
@@ -1131,6 +1158,7 @@ __device__ void write_star(const DevTree& T, WarpCommit<D>& W, const int* __rest
     }
     __syncwarp();
   }
+  return dead;
 }
 
 // Star of one winner, large case: every (facet, face) inserts its ridge into
@@ -1227,6 +1255,21 @@ __device__ __forceinline__ void publish_shared_facets(const DevTree& T, int* F, 
   }
 }
 
+// The same for a small star, from the facets write_star marked (no second
+// read of the kill marks).
+__device__ __forceinline__ void publish_marked(const DevTree& T, int* F, const int* P, const int* IDS, int nfac,
+                                               unsigned dead, int lane) {
+  for (int j = lane, bit = 0; j < nfac; j += 32, ++bit) {
+    if (!((dead >> bit) & 1u)) continue;
+    const int kf = F[6 * j + 5], k = kf >> 2;
+    const int inner = (P[k] << 2) | (kf & 3);
+    T.repl[inner] = (IDS[j] << 2) | (kf & 3);
+    F[6 * j] = IDS[j];
+    F[6 * j + 1] = kf & 3;
+    F[6 * j + 2] = -2;
+  }
+}
+
 // Resolution pass `pass` of a round, check half.  A candidate wins iff it
 // holds every claim on its cavity, no lower candidate rewrites a face of its
 // cavity (claim_n), and no lower candidate's cavity holds one of its outer
@@ -1296,25 +1339,27 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
       int *P, *F, ncav, nfac;
       bool big;
       cand_lists(T, info, P, F, ncav, nfac, big);
+      // the winner's point for its hints, read now so that it arrives while the star is written
+      vdp::FPt fq{};
+      if (MODE != 1 && lane == 0) fq = load_fpt(T, cd.x);
       int base;
       if (MODE != 2) {
+        // the cavity's and the outer simplices' claims are read together:
+        // pool entries in one round trip, all their claims in the next, and
+        // only then decided (a verdict needs every one of them anyway)
         bool ok = true;
-        for (int i = lane; i < ncav; i += 32) {
-          const int s = P[i];
-          if (bad_simp(T, s)) {
-            ok = false;
-            continue;
-          }
-          ok = ok && T.claim_c[s] == key && (MODE == 1 || T.claim_n[s] > key);
-        }
-        for (int j = lane; j < nfac && ok; j += 32) {
-          const int o = F[6 * j + 4];
-          if (o < 0) continue;
-          if (bad_simp(T, o >> 2)) {
-            ok = false;
-            continue;
-          }
-          const unsigned long long ko = T.claim_c[o >> 2];
+        const int nrun = max(ncav, nfac);
+        for (int t = lane; t < nrun; t += 32) {
+          const bool hs = t < ncav, hf = t < nfac;
+          const int s = hs ? P[t] : 0;
+          const int o = hf ? F[6 * t + 4] : -1;
+          const bool sbad = hs && bad_simp(T, s);
+          const bool obad = o >= 0 && bad_simp(T, o >> 2);
+          const unsigned long long kc = (hs && !sbad) ? T.claim_c[s] : key;
+          const unsigned long long kn = (MODE == 0 && hs && !sbad) ? T.claim_n[s] : ~0ull;
+          const unsigned long long ko = (o >= 0 && !obad) ? T.claim_c[o >> 2] : ~0ull;
+          ok = ok && !sbad && !obad && kc == key && (MODE == 1 || kn > key);
+          if (!ok || o < 0) continue;
           if (MODE == 0) {
             ok = ko > key;
           } else if (ko < key) {
@@ -1324,7 +1369,7 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
               ok = false;
               continue;
             }
-            const int* r = F + 6 * j;
+            const int* r = F + 6 * t;
             vdp::FPt fv[NV];
             for (int i = 0; i < NV; ++i) fv[i] = load_fpt(T, r[i]);
             const vdp::FPt fx = load_fpt(T, xv);
@@ -1384,6 +1429,8 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
       }
       int id0;
       const int* IDS;
+      unsigned dead = 0;
+      bool small_star = false;
       if (!big && nfac <= MAXF && ncav <= MAXC) {
         // slot assignment: first facet of cavity simplex k takes k's slot;
         // the other facets take the remaining cavity slots, then fresh ones
@@ -1423,7 +1470,8 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
         // leftover cavity slots become holes pointing into the star
         for (int t = nsec + lane; t < nfree; t += 32)
           store_simplex(T, W.freeslot[t], make_int4(-1, -1, -1, -1), make_int4(id0 << 2, -1, -1, -1));
-        write_star<D>(T, W, F, nfac, cd.x, round, lane);
+        dead = write_star<D>(T, W, F, nfac, cd.x, round, lane);
+        small_star = true;
       } else {
         // large star (spilled search): plain slot assignment, ids in the
         // stretch's vertex-list area (free after the search), ridge table in
@@ -1447,10 +1495,13 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
         // facets shared with another winner's cavity: publish this side's new
         // simplex and remember where the other side's goes (fix_body)
         __syncwarp();
-        publish_shared_facets<false>(T, F, P, IDS, nfac, round, lane);
+        if (small_star)
+          publish_marked(T, F, P, IDS, nfac, dead, lane);
+        else
+          publish_shared_facets<false>(T, F, P, IDS, nfac, round, lane);
       }
       if (lane == 0) {
-        write_hints<D>(T, cd.x, load_fpt(T, cd.x), id0);
+        write_hints<D>(T, cd.x, fq, id0);
         T.cinfo[c].w = ST_DONE;
         T.act[par][cd.w].x = -1;
       }
