@@ -61,10 +61,6 @@ struct Cap;
 #define VD_CAP3_F 192
 #define VD_CAP3_H 256
 #endif
-// 1: k_cavity reads its next item's list entry and record one search ahead
-#ifndef VD_CAVITY_PIPE
-#define VD_CAVITY_PIPE 1
-#endif
 #ifndef VD_CAVITY_MIN_BLOCKS
 #define VD_CAVITY_MIN_BLOCKS 5
 #endif
@@ -917,18 +913,11 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
     const vdp::FPt fq = load_fpt(T, cd.x);
     int4 v0, n0;
     load_simplex(T, cd.y, v0, n0);
-#if VD_CAVITY_PIPE
     if (it + nw < nsurv) {
       c_next = c_after;
       cd_next = T.cand[c_after];
     }
     if (it + 2 * nw < nsurv) c_after = T.wl[0][it + 2 * nw];
-#else
-    if (it + nw < nsurv) {
-      c_next = T.wl[0][it + nw];
-      cd_next = T.cand[c_next];
-    }
-#endif
     if (lane == 0) ++nsearched;
     const unsigned long long key = pe | (unsigned)cd.z;
     cavity_search<D, XT>(T, fast, W.ctl, lane, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
@@ -2016,6 +2005,11 @@ constexpr size_t small_rounds_smem() {
 // of the commit half (MODE 2), 2D and 3D.
 int g_check_wave[2] = {1 << 20, 1 << 20};
 int g_commit_wave[2] = {1 << 20, 1 << 20};
+// Resident blocks of the decide half (XT = 1 form, the larger), 2D and 3D.
+int g_decide_wave[2] = {1 << 20, 1 << 20};
+#ifndef VD_DECIDE_WIDE
+#define VD_DECIDE_WIDE 1
+#endif
 // Grid of k_cavity_big: one 512-thread block per SM.
 int g_big_grid = 1;
 // Grid of the small-round kernel (0: not available).
@@ -2060,6 +2054,8 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
   // the commit half needs little shared memory per warp and few registers,
   // so it runs up to twice the warps of the search (one resident wave)
   const int commit_grid = std::min(L.warps / 2, g_commit_wave[D - 2]);
+  // the decide half (56 registers, 1 KB of shared memory per warp) likewise
+  const int decide_grid = VD_DECIDE_WIDE ? std::min(L.warps / 2, g_decide_wave[D - 2]) : L.warps / 4;
   const int strict_grid = std::min(L.warps / 4, g_check_wave[D - 2]);
   for (int p = 0; p < tu.passes; ++p) {
     const int last = p == tu.passes - 1;
@@ -2070,9 +2066,9 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
     }
     if (tu.adjacent) {
       if (tu.exact_int)
-        k_check<D, 1, 1><<<L.warps / 4, 128, 4 * sizeof(HeadBuf), L.stream>>>(T, p, last, fd.seed, 0);
+        k_check<D, 1, 1><<<decide_grid, 128, 4 * sizeof(HeadBuf), L.stream>>>(T, p, last, fd.seed, 0);
       else
-        k_check<D, 1, 0><<<L.warps / 4, 128, 4 * sizeof(HeadBuf), L.stream>>>(T, p, last, fd.seed, 0);
+        k_check<D, 1, 0><<<decide_grid, 128, 4 * sizeof(HeadBuf), L.stream>>>(T, p, last, fd.seed, 0);
       mark(KT_DECIDE);
       k_check<D, 2, 0><<<commit_grid, 128, 4 * sizeof(WarpCommit<D>), L.stream>>>(T, p, last, fd.seed,
                                                                                   tu.big_block);
@@ -2144,6 +2140,12 @@ int prepare_once() {
   g_big_grid = std::max(1, sms);
   g_commit_wave[1] = std::max(1, sms * c3);
   g_commit_wave[0] = std::max(1, sms * c2);
+  int d3 = 0, d2 = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d3, k_check<3, 1, 1>, 128, 4 * sizeof(HeadBuf)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d2, k_check<2, 1, 1>, 128, 4 * sizeof(HeadBuf)) != cudaSuccess)
+    return E_CUDA;
+  g_decide_wave[1] = std::max(1, sms * d3);
+  g_decide_wave[0] = std::max(1, sms * d2);
   // small-round kernel: one block per SM when a block fits
   int s3 = 0, s2 = 0;
   cudaFuncSetAttribute((const void*)k_rounds_small<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
