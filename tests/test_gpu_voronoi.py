@@ -81,7 +81,30 @@ def test_voronoi_dual_matches_oracle(vd, oracle, dim, n):
         assert abs(r[i] - rr) <= 1e-8 * rr, i
 
 
-def test_voronoi_cells_skip_duplicates_and_cover_batches(vd):
+def test_voronoi_dual_of_a_batched_tree(vd):
+    """A batched tree holds several sets; its dual covers all of them, in the
+    global numbering of vd_simplices, and each set's cells are its own."""
+    sets = [W.uniform_points(n, 3, 300 + n) for n in (400, 1500, 60)]
+    off = np.concatenate([[0], np.cumsum([len(p) for p in sets])])
+    t = vd.DelaunayTree.create(3)
+    t.batch(np.concatenate(sets), off, seed=3)
+    v, nb = t.simplices()
+    E = t.voronoi_edges()
+    assert 2 * len(E) + 4 * len(sets) == 4 * len(v)  # every super simplex keeps its 4 hull faces
+    cells_off, ids = t.voronoi_cells()
+    assert len(cells_off) == off[-1] + 1
+    for s in range(len(sets)):
+        for u in range(off[s], off[s + 1]):
+            cell = ids[cells_off[u]:cells_off[u + 1]]
+            assert len(cell) > 0
+            # a cell's simplices belong to the point's own set: their input vertices share its range
+            verts = v[cell]
+            inner = verts[verts >= 0]
+            assert np.all((inner >= off[s]) & (inner < off[s + 1]))
+    t.close()
+
+
+def test_voronoi_cells_skip_duplicates(vd):
     p = W.uniform_points(500, 3, 77)
     p = np.vstack([p, p[:3]])
     with pytest.warns(RuntimeWarning):
