@@ -478,10 +478,11 @@ def run_c4_ranks(args, world, rank, local):
     import torch.distributed as dist
     from voronoids_gb300 import _native, shard
     from voronoids_gb300 import workloads as W
-    torch.cuda.set_device(local)
+    dev = local % max(torch.cuda.device_count(), 1)  # several ranks may share one GPU (gloo test runs)
+    torch.cuda.set_device(dev)
     backend = os.environ.get("VD_DIST_BACKEND", "nccl")
     dist.init_process_group(backend, init_method="env://")
-    red_dev = torch.device("cuda", local) if backend == "nccl" else torch.device("cpu")
+    red_dev = torch.device("cuda", dev) if backend == "nccl" else torch.device("cpu")
     L = _native.load()
     pts_h, off = W.c4_sets()
     sizes = np.diff(off)
