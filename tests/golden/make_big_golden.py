@@ -15,6 +15,11 @@ Workloads (inputs from ``voronoids_gb300/workloads.py``):
   c2   1,000,000 uniform 3D points, seed 0xD1A00002
   c3   262,144 near-degenerate 3D points (jittered lattice + tight clusters)
   u2   1,000,000 uniform 2D points, seed 0xD1A00006
+  l3   the exact 64^3 lattice scaled by 1/64 (262,144 points; the scaling is exact in
+       binary, so every cell stays cospherical) in a seeded random order: every tie
+       goes through the symbolic perturbation
+  l2   the exact 512^2 lattice scaled by 1/512 (262,144 points, every cell cocircular),
+       likewise
 """
 import hashlib
 import json
@@ -41,7 +46,18 @@ def workloads():
         "c2": lambda: W.c2_points(),
         "c3": lambda: W.c3_points(),
         "u2": lambda: W.uniform_points(1_000_000, 2, W.config_seed(6)),
+        "l3": lambda: lattice(64, 3),
+        "l2": lambda: lattice(512, 2),
     }
+
+
+def lattice(side, dim):
+    """All sites of the side^dim integer lattice scaled by 1/side (side a power of two,
+    so the scaling is exact), in a seeded random order."""
+    assert side & (side - 1) == 0
+    g = W.lattice_points(side, dim) / side
+    order = np.argsort(W.splitmix64(W.config_seed(7) + dim, len(g)), kind="stable")
+    return np.ascontiguousarray(g[order])
 
 
 def digest(edges):

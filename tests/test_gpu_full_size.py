@@ -46,7 +46,7 @@ def build(vd, name, seed):
     return p, t
 
 
-@pytest.mark.parametrize("name", ["c1", "c2", "c3", "u2"])
+@pytest.mark.parametrize("name", ["c1", "c2", "c3", "u2", "l3", "l2"])
 def test_edge_list_digest_matches_oracle(vd, name):
     g = DIGESTS[name]
     p, t = build(vd, name, W.config_seed(2))
