@@ -547,6 +547,8 @@ constexpr int kOffCN = kOffCV + 4 * kBigC;
 constexpr int kOffH = kOffCN + 4 * kBigC;
 constexpr int kOffR = kOffH + kBigH;
 constexpr int kBigInts = kOffR + 4 * kBigR;  // multiple of 4
+// the block search's ready marks (kBigC ints) follow its facet records in the ridge area
+static_assert(2 * kBigF + kBigC <= 4 * kBigR, "block search marks must fit the ridge area");
 // Offset of the facet records after ncav cavity ids: even, so that records
 // (6 ints) start on 8-byte boundaries in an even pool stretch.
 __host__ __device__ constexpr int facets_at(int ncav) { return (ncav + 1) & ~1; }
@@ -574,7 +576,112 @@ __device__ bool hset_find(const int* hk, int hs, int key) {
 
 struct WarpCtl {
   int ncav, nfac, flags, pad;
+  int head, pend;  // block search: next item to hand out, items created and not finished
 };
+
+// Waits of one thread in the block search (cavity_search_dyn), at most:
+// past it the search reports E_INTERNAL and ends instead of waiting on.
+constexpr long long kDynWaitLimit = 1LL << 24;
+
+// Block form of the search (k_cavity_big), without waves: threads take
+// (simplex, face) items from a shared counter as soon as the simplex is
+// stored, so a slow conflict test (FP64 or exact tier) holds up only the
+// items behind it, not a whole wave at a barrier.  `pend` counts items
+// created and not yet finished; a simplex adds its D + 1 items before its
+// parent item finishes and before it is marked ready, so the count reaches
+// zero only when the region is complete.  rdy[k] marks cavity entry k as
+// stored (rdy: S.maxc ints of the caller's stretch).  Same region, facets
+// and capacity flags as the wave form; only the order of the lists differs.
+template <int D, int XT>
+__device__ void cavity_search_dyn(const DevTree& T, const CavStore& S, WarpCtl& ctl, int* rdy, int rank,
+                                  int start, int4 v0, int4 n0, int qv, const vdp::FPt& fq, vdp::Tally& tl,
+                                  int& perr, unsigned long long& ntests) {
+  constexpr int NV = D + 1;
+  const int G = (int)blockDim.x;
+  for (int i = rank; i < S.hs; i += G) S.hk[i] = -1;
+  for (int i = rank; i < S.maxc; i += G) rdy[i] = 0;
+  __syncthreads();
+  if (rank == 0) {
+    ctl.ncav = 1;
+    ctl.nfac = 0;
+    ctl.flags = 0;
+    ctl.head = 0;
+    ctl.pend = NV;
+    S.cav[0] = start;
+    S.cv[0] = v0;
+    S.cn[0] = n0;
+    hset_insert(S.hk, S.hs, start);
+    rdy[0] = 1;
+  }
+  __syncthreads();
+  long long waits = 0;
+  while (true) {
+    const int it = atomicAdd(&ctl.head, 1);
+    const int k = it / NV, f = it - k * NV;
+    bool ready = false;
+    while (true) {
+      if (k < S.maxc && k < *(volatile int*)&ctl.ncav && *(volatile int*)&rdy[k]) {
+        ready = true;
+        break;
+      }
+      if (*(volatile int*)&ctl.pend == 0 || *(volatile int*)&ctl.flags) break;
+      if (++waits > kDynWaitLimit) {
+        set_error(T.ctr, E_INTERNAL);
+        atomicOr(&ctl.flags, 4);
+        break;
+      }
+      __nanosleep(32);
+    }
+    if (!ready) break;
+    __threadfence_block();  // the entry's records after its ready mark
+    const int code = get4(__ldcg(&S.cn[k]), f);  // from L2: another thread stored it
+    bool facet = code < 0;
+    const bool broken = !facet && bad_simp(T, code >> 2);
+    if (broken) set_error(T.ctr, E_INTERNAL);
+    if (!facet && !broken) {
+      const int nb = code >> 2;
+      if (!hset_find(S.hk, S.hs, nb)) {
+        int4 vv, nn;
+        load_simplex(T, nb, vv, nn);
+        vdp::FPt fv[NV];
+        int kv[NV];
+        for (int j = 0; j < NV; ++j) {
+          kv[j] = get4(vv, j);
+          fv[j] = load_fpt(T, kv[j]);
+        }
+        ++ntests;
+        auto load64 = [&](vdp::VPt* v64, vdp::VPt& q64) {
+          for (int j = 0; j < NV; ++j) v64[j] = load_pt(T, kv[j]);
+          q64 = load_pt(T, qv);
+        };
+        if (vdp::in_conflict_hl<D, XT>(fv, kv, fq, qv, tl, perr, load64)) {
+          if (hset_insert(S.hk, S.hs, nb)) {
+            const int s = atomicAdd(&ctl.ncav, 1);
+            if (s < S.maxc) {
+              S.cav[s] = nb;
+              S.cv[s] = vv;
+              S.cn[s] = nn;
+              atomicAdd(&ctl.pend, NV);  // before the mark: the parent item is still counted
+              __threadfence_block();
+              *(volatile int*)&rdy[s] = 1;
+            } else {
+              atomicOr(&ctl.flags, 1);
+            }
+          }
+        } else {
+          facet = true;
+        }
+      }
+    }
+    if (facet) {
+      const int s = atomicAdd(&ctl.nfac, 1);
+      if (s < S.maxf) S.fr[s] = make_int2(code, (k << 2) | f);
+      else atomicOr(&ctl.flags, 2);
+    }
+    atomicSub(&ctl.pend, 1);
+  }
+  __syncthreads();
+}
 
 // Breadth-first search of the conflict region of candidate q from the
 // simplex that contains it; all 32 lanes of the warp call this.  Returns
@@ -846,8 +953,11 @@ __device__ void big_search(const DevTree& T, WarpCtl& ctl, int rank, int c, int4
   // until the commit) and are expanded to P + kOffF afterwards
   const CavStore big{P, reinterpret_cast<int4*>(P + kOffCV), reinterpret_cast<int4*>(P + kOffCN),
                      P + kOffH, reinterpret_cast<int2*>(P + kOffR), kBigC, kBigF, kBigH};
-  cavity_search<D, XT, BLOCK>(T, big, ctl, rank, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
-  const int ncav = *(volatile int*)&ctl.ncav, nfac = *(volatile int*)&ctl.nfac;
+  if constexpr (BLOCK)
+    cavity_search_dyn<D, XT>(T, big, ctl, P + kOffR + 2 * kBigF, rank, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
+  else
+    cavity_search<D, XT, false>(T, big, ctl, rank, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
+  const int ncav = min(*(volatile int*)&ctl.ncav, kBigC), nfac = min(*(volatile int*)&ctl.nfac, kBigF);
   const int flags = *(volatile int*)&ctl.flags;
   sync();
   if (flags) {
