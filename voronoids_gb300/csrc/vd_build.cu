@@ -547,8 +547,9 @@ constexpr int kOffCN = kOffCV + 4 * kBigC;
 constexpr int kOffH = kOffCN + 4 * kBigC;
 constexpr int kOffR = kOffH + kBigH;
 constexpr int kBigInts = kOffR + 4 * kBigR;  // multiple of 4
-// the block search's ready marks (kBigC ints) follow its facet records in the ridge area
-static_assert(2 * kBigF + kBigC <= 4 * kBigR, "block search marks must fit the ridge area");
+// Dynamic shared memory of k_cavity_big: the id set (kBigH ints) and the
+// ready marks (kBigC ints) of its block search.
+constexpr int kBigSmem = (kBigH + kBigC) * (int)sizeof(int);
 // Offset of the facet records after ncav cavity ids: even, so that records
 // (6 ints) start on 8-byte boundaries in an even pool stretch.
 __host__ __device__ constexpr int facets_at(int ncav) { return (ncav + 1) & ~1; }
@@ -924,7 +925,7 @@ __device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int
 // warp (BLOCK = false) or the whole block (k_cavity_big) runs it.  The
 // stretch offset is broadcast through ctl.pad.
 template <int D, int XT, bool BLOCK>
-__device__ void big_search(const DevTree& T, WarpCtl& ctl, int rank, int c, int4 cd, int4 v0, int4 n0,
+__device__ void big_search(const DevTree& T, WarpCtl& ctl, int* bsm, int rank, int c, int4 cd, int4 v0, int4 n0,
                            const vdp::FPt& fq, unsigned long long key, int adjacent, vdp::Tally& tl, int& perr,
                            unsigned long long& ntests, int& mcav, int& mfac) {
   auto sync = [] {
@@ -951,10 +952,11 @@ __device__ void big_search(const DevTree& T, WarpCtl& ctl, int rank, int c, int4
   int* P = T.pool + off;
   // the search's 2-int facet records go to the ridge-table area (unused
   // until the commit) and are expanded to P + kOffF afterwards
+  // the block search keeps its id set and ready marks in shared memory (bsm)
   const CavStore big{P, reinterpret_cast<int4*>(P + kOffCV), reinterpret_cast<int4*>(P + kOffCN),
-                     P + kOffH, reinterpret_cast<int2*>(P + kOffR), kBigC, kBigF, kBigH};
+                     BLOCK ? bsm : P + kOffH, reinterpret_cast<int2*>(P + kOffR), kBigC, kBigF, kBigH};
   if constexpr (BLOCK)
-    cavity_search_dyn<D, XT>(T, big, ctl, P + kOffR + 2 * kBigF, rank, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
+    cavity_search_dyn<D, XT>(T, big, ctl, bsm + kBigH, rank, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
   else
     cavity_search<D, XT, false>(T, big, ctl, rank, cd.y, v0, n0, cd.x, fq, tl, perr, ntests);
   const int ncav = min(*(volatile int*)&ctl.ncav, kBigC), nfac = min(*(volatile int*)&ctl.nfac, kBigF);
@@ -1043,7 +1045,8 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
           T.cinfo[c] = make_int4(0, 0, 0, ST_BIG);
         }
       } else {
-        big_search<D, XT, false>(T, W.ctl, lane, c, cd, v0, n0, fq, key, adjacent, tl, perr, ntests, mcav, mfac);
+        big_search<D, XT, false>(T, W.ctl, nullptr, lane, c, cd, v0, n0, fq, key, adjacent, tl, perr, ntests, mcav,
+                                 mfac);
       }
       __syncwarp();
       continue;
@@ -1100,6 +1103,7 @@ __global__ void __launch_bounds__(128, VD_CAVITY_MIN_BLOCKS) k_cavity(DevTree T,
 template <int D, int XT>
 __global__ void __launch_bounds__(512, 1) k_cavity_big(DevTree T, int adjacent) {
   __shared__ WarpCtl ctl;
+  extern __shared__ int bsm[];  // kBigSmem bytes: the search's id set, then its ready marks
   const int n = T.ctr->nbig;
   if (n == 0) return;
   const unsigned long long pe = pass_epoch(T.ctr->round, 0);
@@ -1112,7 +1116,7 @@ __global__ void __launch_bounds__(512, 1) k_cavity_big(DevTree T, int adjacent) 
     const vdp::FPt fq = load_fpt(T, cd.x);
     int4 v0, n0;
     load_simplex(T, cd.y, v0, n0);
-    big_search<D, XT, true>(T, ctl, threadIdx.x, c, cd, v0, n0, fq, pe | (unsigned)cd.z, adjacent, tl, perr, ntests,
+    big_search<D, XT, true>(T, ctl, bsm, threadIdx.x, c, cd, v0, n0, fq, pe | (unsigned)cd.z, adjacent, tl, perr, ntests,
                             mcav, mfac);
   }
   if (perr) set_error(T.ctr, E_PRECISION);
@@ -2156,9 +2160,9 @@ void round_impl(const DevTree& T, const Launch& L, const Tuning& tu, const Feed&
   // by whole blocks (the host turns it on once a call has spilled searches)
   if (tu.big_block) {
     if (tu.exact_int)
-      k_cavity_big<D, 1><<<g_big_grid, 512, 0, L.stream>>>(T, tu.adjacent);
+      k_cavity_big<D, 1><<<g_big_grid, 512, kBigSmem, L.stream>>>(T, tu.adjacent);
     else
-      k_cavity_big<D, 0><<<g_big_grid, 512, 0, L.stream>>>(T, tu.adjacent);
+      k_cavity_big<D, 0><<<g_big_grid, 512, kBigSmem, L.stream>>>(T, tu.adjacent);
     mark(KT_BIG);
   }
   // the commit half needs little shared memory per warp and few registers,
@@ -2235,6 +2239,10 @@ int prepare_once() {
   attr((const void*)k_check<2, 0, 0>, 4 * (int)sizeof(WarpCommit<2>));
   attr((const void*)k_check<2, 0, 1>, 4 * (int)sizeof(WarpCommit<2>));
   attr((const void*)k_check<2, 2, 0>, 4 * (int)sizeof(WarpCommit<2>));
+  attr((const void*)k_cavity_big<3, 0>, kBigSmem);
+  attr((const void*)k_cavity_big<3, 1>, kBigSmem);
+  attr((const void*)k_cavity_big<2, 0>, kBigSmem);
+  attr((const void*)k_cavity_big<2, 1>, kBigSmem);
   if (e != cudaSuccess) return E_CUDA;
   // k_check is a grid-stride loop: one resident wave avoids a ragged second
   int dev = 0, sms = 0, b3 = 0, b2 = 0, c3 = 0, c2 = 0;
