@@ -244,6 +244,24 @@ __device__ __forceinline__ void write_hints(const DevTree& T, int vid, const vdp
   for (int l = 0; l <= g.hint_levels; ++l) T.hint[hint_at<D>(g, ic, l)] = slot;
 }
 
+// The same with coarse levels sampled: a cell of level l covers 2^(D (L - l))
+// cells of the finest level L, so it is written with probability
+// 2^-(D (L - l)) (from the low bits of the point's priority).  Every cell
+// then takes about as many writes as a finest cell, instead of every winner
+// of a round storing to the one cell of level 0.  With `all` (while the
+// tree is small and most fine cells are still empty) every level is written.
+template <int D>
+__device__ __forceinline__ void write_hints_sampled(const DevTree& T, int vid, const vdp::FPt& q, int slot,
+                                                   unsigned pr, bool all) {
+  const SetGeo& g = T.sets[set_index(T, vid)];
+  int ic[3];
+  hint_cell<D>(g, q, ic);
+  for (int l = 0; l <= g.hint_levels; ++l) {
+    const int sh = D * (g.hint_levels - l);
+    if (all || sh == 0 || (sh < 32 && (pr & ((1u << sh) - 1u)) == 0)) T.hint[hint_at<D>(g, ic, l)] = slot;
+  }
+}
+
 // Priority levels.  Level k holds the points with thr[k-1] <= priority <
 // thr[k]; the thresholds grow geometrically, so level sizes do too (the
 // biased randomized insertion order: every prefix of levels is a random
@@ -1418,6 +1436,7 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
   }
   const unsigned long long pe = pass_epoch(round, pass);
   const int par = round & 1;
+  const bool hint_all = T.ctr->ninserted < T.hint_all_below;
   unsigned long long nwon = 0, ncreated = 0, nkilled = 0;
   int nholes = 0;
   vdp::Tally tl = {0, 0, 0, 0};
@@ -1604,7 +1623,7 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
           publish_shared_facets<false>(T, F, P, IDS, nfac, round, lane);
       }
       if (lane == 0) {
-        write_hints<D>(T, cd.x, fq, id0);
+        write_hints_sampled<D>(T, cd.x, fq, id0, (unsigned)cd.z, hint_all);
         T.cinfo[c].w = ST_DONE;
         T.act[par][cd.w].x = -1;
       }

@@ -774,6 +774,8 @@ bool launch_chunk_graph(vd_tree* t, const vd::Launch& L, int chunk, const vd::Fe
 int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
   const vd::Feed fd_main{seed, (float)t->ratio};
   const vd::Feed fd_early{seed, (float)std::max(t->ratio, t->early_ratio)};
+  // winners refresh every level of the location hints during the early phase
+  t->T.hint_all_below = (int)std::min<int64_t>(t->early_until, 0x7fffffff);
   const vd::Tuning tu_main = t->tuning;
   vd::Tuning tu_early = t->tuning;
   tu_early.thin = t->early_thin;

@@ -164,6 +164,7 @@ struct DevTree {
   int cap_pool;
   int cap_cand;
   int cap_dups;
+  int hint_all_below;  // winners write every hint level while fewer points are inserted
 };
 
 __host__ __device__ inline unsigned long long epoch(int round) {
