@@ -2305,11 +2305,17 @@ int prepare_once() {
 }  // namespace
 
 // Once per process (trees may be created from several host threads).
+// Function attributes (dynamic shared memory above 48 KB) belong to a device's
+// context, so they are set once per device the process uses.
 int prepare_round_kernels() {
-  static std::once_flag once;
-  static int rc = E_CUDA;
-  std::call_once(once, [] { rc = prepare_once(); });
-  return rc;
+  constexpr int kMaxDevices = 64;
+  static std::mutex mu;
+  static int state[kMaxDevices] = {};  // 0 not yet, 1 ready, -1 failed
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return E_CUDA;
+  std::lock_guard<std::mutex> lock(mu);
+  if (state[dev] == 0) state[dev] = prepare_once() == E_OK ? 1 : -1;
+  return state[dev] == 1 ? E_OK : E_CUDA;
 }
 
 int launch_small_rounds(const DevTree& T, cudaStream_t stream, int dim, const Tuning& tu, const Feed& fd,
