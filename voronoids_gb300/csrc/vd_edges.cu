@@ -5,10 +5,11 @@
 // (PyDelauanyTree.simplices, src/lib.rs:87-100); the parity contract of this
 // build is the sorted edge list derived from it.  Instead of a global sort of
 // all (simplex, edge) instances, instances are bucketed by their smaller
-// endpoint (counting pass + exclusive scan + scatter), each bucket (about 40
-// entries per vertex in 3D, 6 in 2D) is sorted and de-duplicated by one warp
-// in shared memory, and a second scan places the unique edges.  Buckets longer
-// than a warp's buffer are sorted by a block in global memory.
+// endpoint (counting pass + exclusive scan + scatter), each bucket is sorted
+// and de-duplicated by one warp in shared memory, and a second scan places the
+// unique edges.  Buckets longer than a warp's buffer are sorted by a block in
+// global memory.  A simplex emits an edge only where the emission rule below
+// picks it (about 2.6 instances per edge in 3D instead of ~5.2, one in 2D).
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -93,6 +94,22 @@ void exclusive_scan(const int* in, int* out, long long n, int* tmp, cudaStream_t
 }
 
 // ---- edge instances ---------------------------------------------------------
+// Simplex s emits its edge (v[i], v[j]) only if s is below its neighbours
+// across the faces that contain the edge (the faces opposite the other
+// vertices; a hull face counts as no neighbour).  Around an edge the
+// simplices form a ring (2D: a pair) in which each one's neighbours across
+// those faces are its two ring neighbours, so the ring's lowest slot always
+// emits: every edge still appears, about a third as often in 3D and exactly
+// once in 2D, which shrinks the buckets to sort.
+template <int NV>
+__device__ __forceinline__ bool emits(int s, const int* nb, int i, int j) {
+  for (int k = 0; k < NV; ++k) {
+    if (k == i || k == j) continue;
+    if (nb[k] >= 0 && (nb[k] >> 2) < s) return false;
+  }
+  return true;
+}
+
 template <int D>
 __global__ void k_edge_count(DevTree T, int nsimp, int n_in, int* cnt) {
   constexpr int NV = D + 1;
@@ -100,11 +117,13 @@ __global__ void k_edge_count(DevTree T, int nsimp, int n_in, int* cnt) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsimp; s += gridDim.x * blockDim.x) {
     const int4 v = reinterpret_cast<const int4*>(T.simp + s)[0];
     if (v.x < 0) continue;
+    const int4 n = reinterpret_cast<const int4*>(T.simp + s)[1];
     const int a[4] = {v.x, v.y, v.z, v.w};
+    const int nb[4] = {n.x, n.y, n.z, n.w};
     for (int i = 0; i < NV; ++i)
       for (int j = i + 1; j < NV; ++j) {
         int x = a[i], y = a[j];
-        if (x < NS || y < NS) continue;
+        if (x < NS || y < NS || !emits<NV>(s, nb, i, j)) continue;
         if (max(x, y) - NS >= n_in) {
           set_error(T.ctr, E_INTERNAL);
           continue;
@@ -121,11 +140,13 @@ __global__ void k_edge_fill(DevTree T, int nsimp, int n_in, int* cnt, const int*
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsimp; s += gridDim.x * blockDim.x) {
     const int4 v = reinterpret_cast<const int4*>(T.simp + s)[0];
     if (v.x < 0) continue;
+    const int4 n = reinterpret_cast<const int4*>(T.simp + s)[1];
     const int a[4] = {v.x, v.y, v.z, v.w};
+    const int nb[4] = {n.x, n.y, n.z, n.w};
     for (int i = 0; i < NV; ++i)
       for (int j = i + 1; j < NV; ++j) {
         int x = a[i], y = a[j];
-        if (x < NS || y < NS) continue;
+        if (x < NS || y < NS || !emits<NV>(s, nb, i, j)) continue;
         int u = min(x, y) - NS, w = max(x, y) - NS;
         if (w >= n_in) continue;
         int k = atomicSub(cnt + u, 1) - 1;  // cnt returns to 0
