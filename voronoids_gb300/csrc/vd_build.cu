@@ -133,17 +133,18 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
   for (int o = 16; o; o >>= 1) v += __shfl_down_sync(FULL, v, o);
   return v;
 }
-__device__ void flush_tally(Counters* c, const vdp::Tally& t, unsigned long long tests,
-                            unsigned long long walk) {
-  unsigned long long a = warp_sum(t.f32), b = warp_sum(t.f64), e = warp_sum(t.exact),
-                     s = warp_sum(t.sos), x = warp_sum(tests), w = warp_sum(walk);
+// Statistics: each warp adds its sums to one of kStatStripes copies of the
+// counters, so that the warps of a launch, finishing together, do not all
+// add to the same address (those atomics serialise in L2: about 3 % of a
+// 1M-point build).  Counts that steer the build (winners, inserted) are
+// summed per block instead (shared memory, one atomic per block).
+__device__ void flush_tally(Counters* c, const vdp::Tally& t, unsigned tests, unsigned walk) {
+  const unsigned long long v[STAT_COUNT] = {warp_sum(t.f32), warp_sum(t.f64), warp_sum(t.exact),
+                                            warp_sum(t.sos), warp_sum(tests), warp_sum(walk)};
   if ((threadIdx.x & 31) == 0) {
-    if (a) atomicAdd(&c->tally[0], a);
-    if (b) atomicAdd(&c->tally[1], b);
-    if (e) atomicAdd(&c->tally[2], e);
-    if (s) atomicAdd(&c->tally[3], s);
-    if (x) atomicAdd(&c->cavity_tests, x);
-    if (w) atomicAdd(&c->walk, w);
+    const unsigned stripe = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) % kStatStripes;
+    for (int i = 0; i < STAT_COUNT; ++i)
+      if (v[i]) atomicAdd(&c->stat[stripe][i], v[i]);
   }
 }
 
@@ -394,7 +395,7 @@ __device__ __forceinline__ void activate_body(DevTree T, unsigned long long seed
   const int lo = T.ctr->feed_lo, n = T.ctr->feed_hi - lo;
   vdp::Tally tl = {0, 0, 0, 0};
   int perr = 0;
-  unsigned long long walk = 0;
+  unsigned walk = 0;
   const int cap = 1 << 16;
   for (int b = bid * blockDim.x; b < n; b += nblk * blockDim.x) {
     const int i = b + threadIdx.x;
@@ -510,8 +511,16 @@ __device__ __forceinline__ void pick_body(DevTree T, int thin, int bid, int nblk
         if (nb[f] >= 0 && !bad_simp(T, nb[f] >> 2)) atomicMin(T.thin + (nb[f] >> 2), key);
     }
   }
-  ncand = warp_sum(ncand);
-  if ((threadIdx.x & 31) == 0 && ncand) atomicAdd(&T.ctr->candidates, ncand);
+  {
+    __shared__ unsigned long long nb_acc;
+    ncand = warp_sum(ncand);
+    __syncthreads();
+    if (threadIdx.x == 0) nb_acc = 0;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0 && ncand) atomicAdd(&nb_acc, ncand);
+    __syncthreads();
+    if (threadIdx.x == 0 && nb_acc) atomicAdd(&T.ctr->candidates, nb_acc);
+  }
 }
 template <int D>
 __global__ void k_pick(DevTree T, int thin) { pick_body<D>(T, thin, blockIdx.x, gridDim.x); }
@@ -614,7 +623,7 @@ constexpr long long kDynWaitLimit = 1LL << 24;
 template <int D, int XT>
 __device__ void cavity_search_dyn(const DevTree& T, const CavStore& S, WarpCtl& ctl, int* rdy, int rank,
                                   int start, int4 v0, int4 n0, int qv, const vdp::FPt& fq, vdp::Tally& tl,
-                                  int& perr, unsigned long long& ntests) {
+                                  int& perr, unsigned& ntests) {
   constexpr int NV = D + 1;
   const int G = (int)blockDim.x;
   for (int i = rank; i < S.hs; i += G) S.hk[i] = -1;
@@ -712,7 +721,7 @@ __device__ void cavity_search_dyn(const DevTree& T, const CavStore& S, WarpCtl& 
 template <int D, int XT, bool BLOCK = false>
 __device__ void cavity_search(const DevTree& T, const CavStore& S, WarpCtl& ctl, int lane, int start,
                               int4 v0, int4 n0, int qv, const vdp::FPt& fq, vdp::Tally& tl, int& perr,
-                              unsigned long long& ntests) {
+                              unsigned& ntests) {
   constexpr int NV = D + 1;
   const int G = BLOCK ? (int)blockDim.x : 32;
   auto sync = [] {
@@ -945,7 +954,7 @@ __device__ __forceinline__ void claim_region(const DevTree& T, const int* P, int
 template <int D, int XT, bool BLOCK>
 __device__ void big_search(const DevTree& T, WarpCtl& ctl, int* bsm, int rank, int c, int4 cd, int4 v0, int4 n0,
                            const vdp::FPt& fq, unsigned long long key, int adjacent, vdp::Tally& tl, int& perr,
-                           unsigned long long& ntests, int& mcav, int& mfac) {
+                           unsigned& ntests, int& mcav, int& mfac) {
   auto sync = [] {
     if (BLOCK)
       __syncthreads();
@@ -1021,7 +1030,8 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
   const unsigned long long pe = pass_epoch(round, 0);
   vdp::Tally tl = {0, 0, 0, 0};
   int perr = 0;
-  unsigned long long ntests = 0, nsearched = 0, nspill = 0;
+  unsigned ntests = 0;
+  unsigned long long nsearched = 0, nspill = 0;
   int mcav = 0, mfac = 0;
   // pool space is taken in per-warp chunks (one atomic per chunk, not per
   // candidate); what a warp leaves unused is dropped with the round's pool
@@ -1101,13 +1111,27 @@ __device__ __forceinline__ void cavity_body(DevTree T, int adjacent, int bid, in
   }
   if (perr) set_error(T.ctr, E_PRECISION);
   flush_tally(T.ctr, tl, ntests, 0);
-  nsearched = warp_sum(nsearched);
-  nspill = warp_sum(nspill);
-  if (lane == 0) {
-    if (nsearched) atomicAdd(&T.ctr->searched, nsearched);
-    if (nspill) atomicAdd(&T.ctr->spilled, nspill);
-    if (mcav) atomicMax(&T.ctr->max_cav, mcav);
-    if (mfac) atomicMax(&T.ctr->max_fac, mfac);
+  {
+    __shared__ unsigned long long cs[2];
+    __shared__ int cm[2];
+    nsearched = warp_sum(nsearched);
+    nspill = warp_sum(nspill);
+    __syncthreads();
+    if (threadIdx.x == 0) cs[0] = cs[1] = 0, cm[0] = cm[1] = 0;
+    __syncthreads();
+    if (lane == 0) {
+      if (nsearched) atomicAdd(&cs[0], nsearched);
+      if (nspill) atomicAdd(&cs[1], nspill);
+      if (mcav) atomicMax(&cm[0], mcav);
+      if (mfac) atomicMax(&cm[1], mfac);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (cs[0]) atomicAdd(&T.ctr->searched, cs[0]);
+      if (cs[1]) atomicAdd(&T.ctr->spilled, cs[1]);
+      if (cm[0]) atomicMax(&T.ctr->max_cav, cm[0]);
+      if (cm[1]) atomicMax(&T.ctr->max_fac, cm[1]);
+    }
   }
 }
 template <int D, int XT>
@@ -1127,7 +1151,7 @@ __global__ void __launch_bounds__(512, 1) k_cavity_big(DevTree T, int adjacent) 
   const unsigned long long pe = pass_epoch(T.ctr->round, 0);
   vdp::Tally tl = {0, 0, 0, 0};
   int perr = 0, mcav = 0, mfac = 0;
-  unsigned long long ntests = 0;
+  unsigned ntests = 0;
   for (int i = blockIdx.x; i < n; i += gridDim.x) {
     const int c = T.bigc[i];
     const int4 cd = T.cand[c];
@@ -1635,17 +1659,29 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
   }
   if (perr) set_error(T.ctr, E_PRECISION);
   if (MODE == 1) flush_tally(T.ctr, tl, 0, 0);
-  if (lane == 0) {
-    if (MODE != 2 && gw < T.cap_wchunk) T.wchunk[gw] = chunk;
-    if (nwon) {
-      atomicAdd(&T.ctr->won[min(pass, kPassesMax - 1)], nwon);
-      atomicAdd(&T.ctr->winners, (int)nwon);
-      atomicAdd(&T.ctr->ninserted, (int)nwon);
+  if (lane == 0 && MODE != 2 && gw < T.cap_wchunk) T.wchunk[gw] = chunk;
+  {
+    // per-warp counts (the same in every lane) summed over the block
+    __shared__ unsigned long long ks[4];  // won, created, killed, holes
+    __syncthreads();
+    if (threadIdx.x < 4) ks[threadIdx.x] = 0;
+    __syncthreads();
+    if (lane == 0) {
+      if (nwon) atomicAdd(&ks[0], nwon);
+      if (ncreated) atomicAdd(&ks[1], ncreated);
+      if (nkilled) atomicAdd(&ks[2], nkilled);
+      if (nholes) atomicAdd(&ks[3], (unsigned long long)nholes);
     }
-    if (ncreated) {
-      atomicAdd(&T.ctr->created, ncreated);
-      atomicAdd(&T.ctr->killed, nkilled);
-      if (nholes) atomicAdd(&T.ctr->holes, nholes);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (ks[0]) {
+        atomicAdd(&T.ctr->won[min(pass, kPassesMax - 1)], ks[0]);
+        atomicAdd(&T.ctr->winners, (int)ks[0]);
+        atomicAdd(&T.ctr->ninserted, (int)ks[0]);
+      }
+      if (ks[1]) atomicAdd(&T.ctr->created, ks[1]);
+      if (ks[2]) atomicAdd(&T.ctr->killed, ks[2]);
+      if (ks[3]) atomicAdd(&T.ctr->holes, (int)ks[3]);
     }
   }
 }
@@ -1789,7 +1825,7 @@ __device__ __forceinline__ void relocate_body(DevTree T, int bid, int nblk) {
   const unsigned long long ep1 = epoch(round + 1);
   vdp::Tally tl = {0, 0, 0, 0};
   int perr = 0;
-  unsigned long long walk = 0;
+  unsigned walk = 0;
   const int cap = 4096;
   for (int b = bid * blockDim.x; b < n; b += nblk * blockDim.x) {
     const int i = b + threadIdx.x;
@@ -2048,7 +2084,7 @@ __global__ void __launch_bounds__(32) k_insert_one(DevTree T, double x, double y
   const int start = s_start;
   int4 v0, n0;
   load_simplex(T, start, v0, n0);
-  unsigned long long ntests = 0;
+  unsigned ntests = 0;
   const CavStore S{C.cav, C.cv, C.cn, C.hkey, C.fr, MAXC, MAXF, HS};
   cavity_search<D, 0>(T, S, C.ctl, lane, start, v0, n0, vid, fq, tl, perr, ntests);
   if (C.ctl.flags) {  // too large for the warp: the rounds insert it

@@ -786,7 +786,7 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
   Counters& h = *t->hctr;
   int64_t active = 0, fed = 0, done = t->hctr->ninserted;
   // exact tests of this call so far decide the form of the conflict-test kernels
-  const unsigned long long exact0 = h.tally[2];
+  const unsigned long long exact0 = vd::stat_total(h, vd::STAT_EXACT);
   bool exact_int = t->exact_mode == 2;
   // oversized searches and stars go to whole-block kernels once the call has
   // had one (until then a warp redoes them, and the extra kernels are not run)
@@ -839,7 +839,7 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
                               (int64_t)h.candidates,
                               (int64_t)h.searched,
                               (int64_t)h.ninserted,
-                              (int64_t)h.cavity_tests,
+                              (int64_t)vd::stat_total(h, vd::STAT_TESTS),
                               us,
                               (int64_t)h.nact[r & 1]};
       t->trace_rows.insert(t->trace_rows.end(), row, row + 8);
@@ -848,7 +848,8 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
       rc = h.err;
       break;
     }
-    if (t->exact_mode == 0 && (int64_t)(h.tally[2] - exact0) >= t->exact_switch) exact_int = true;
+    if (t->exact_mode == 0 && (int64_t)(vd::stat_total(h, vd::STAT_EXACT) - exact0) >= t->exact_switch)
+      exact_int = true;
     if (h.spilled > spilled0) big_block = true;
     active = h.nact[r & 1];
     fed = h.feed_hi;
@@ -1421,12 +1422,12 @@ int vd_get_stats(vd_tree* t, vd_stats* s) {
   s->killed = (int64_t)h.killed;
   s->max_cavity = h.max_cav;
   s->max_facets = h.max_fac;
-  s->pred_f32 = (int64_t)h.tally[0];
-  s->pred_f64 = (int64_t)h.tally[1];
-  s->pred_exact = (int64_t)h.tally[2];
-  s->pred_sos = (int64_t)h.tally[3];
-  s->walk_steps = (int64_t)h.walk;
-  s->cavity_tests = (int64_t)h.cavity_tests;
+  s->pred_f32 = (int64_t)vd::stat_total(h, vd::STAT_F32);
+  s->pred_f64 = (int64_t)vd::stat_total(h, vd::STAT_F64);
+  s->pred_exact = (int64_t)vd::stat_total(h, vd::STAT_EXACT);
+  s->pred_sos = (int64_t)vd::stat_total(h, vd::STAT_SOS);
+  s->walk_steps = (int64_t)vd::stat_total(h, vd::STAT_WALK);
+  s->cavity_tests = (int64_t)vd::stat_total(h, vd::STAT_TESTS);
   s->deferred_overflow = h.overflow;
   s->deferred_pool = h.pool_overflow;
   s->candidates = (int64_t)h.candidates;

@@ -63,6 +63,11 @@ enum : int {
   E_RANGE = 13,
 };
 
+// Statistics counters kept in stripes (see Counters::stat).
+constexpr int kStatStripes = 32;
+constexpr int kStatPad = 16;  // one 128-byte line per stripe
+enum : int { STAT_F32 = 0, STAT_F64 = 1, STAT_EXACT = 2, STAT_SOS = 3, STAT_TESTS = 4, STAT_WALK = 5, STAT_COUNT = 6 };
+
 struct Counters {
   int nact[2];        // active (uninserted) points, by round parity
   int ncand;          // candidates of the current round
@@ -82,9 +87,11 @@ struct Counters {
   int holes;          // dead slots left when a cavity had more simplices than facets
   unsigned long long created;  // simplices created (total)
   unsigned long long killed;   // simplices removed (total)
-  unsigned long long tally[4]; // predicate decisions: f32, f64, exact, sos
-  unsigned long long walk;     // relocation walk steps
-  unsigned long long cavity_tests;  // conflict tests in cavity searches
+  // statistics in kStatStripes copies, added to by warps in turn (one
+  // counter for a whole launch's warps would serialise their atomics):
+  // predicate decisions (f32, f64, exact, sos), conflict tests in cavity
+  // searches, walk steps; stat_total() sums the copies
+  unsigned long long stat[kStatStripes][kStatPad];
   unsigned long long candidates;    // nominated points (all rounds)
   unsigned long long searched;      // candidates that passed the thinning claim
   unsigned long long won[kPassesMax];  // winners per resolution pass
@@ -102,6 +109,13 @@ struct Counters {
   int bar_abort, coop_go;
   int single;                       // outcome of the last one-point insertion (k_insert_one)
 };
+
+// Sum of a striped statistics counter (host or device).
+__host__ __device__ inline unsigned long long stat_total(const Counters& c, int k) {
+  unsigned long long s = 0;
+  for (int i = 0; i < kStatStripes; ++i) s += c.stat[i][k];
+  return s;
+}
 
 // Points of one insertion call are split into priority levels of
 // geometrically growing size; at most this many.

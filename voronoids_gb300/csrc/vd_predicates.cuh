@@ -76,7 +76,7 @@ struct alignas(32) VPt {
 
 // Per-thread counters of which tier decided each predicate.
 struct Tally {
-  unsigned long long f32, f64, exact, sos;
+  unsigned f32, f64, exact, sos;  // per thread and launch: 32 bits suffice and keep registers free
 };
 
 enum : int { PRED_ERR_XCAP = 1 };
