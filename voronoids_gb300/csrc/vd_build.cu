@@ -1685,8 +1685,20 @@ __device__ __forceinline__ void check_body(DevTree T, int pass, int last, unsign
     }
   }
 }
+// resident 128-thread blocks per SM asked of the decide / commit kernels (0:
+// no bound).  Without one the compiler keeps them at 48-56 registers and
+// spills; with 6 (at most 85 registers) the commit half has none and the
+// 1M-point build is 1.6 % faster than with no bound (4 and 8 measured too).
+#ifndef VD_CHECK_MIN_BLOCKS
+#define VD_CHECK_MIN_BLOCKS 6
+#endif
+#if VD_CHECK_MIN_BLOCKS > 0
+#define VD_CHECK_BOUNDS __launch_bounds__(128, VD_CHECK_MIN_BLOCKS)
+#else
+#define VD_CHECK_BOUNDS __launch_bounds__(128)
+#endif
 template <int D, int MODE, int XT>
-__global__ void __launch_bounds__(128) k_check(DevTree T, int pass, int last, unsigned long long seed, int defer_big) {
+__global__ void VD_CHECK_BOUNDS k_check(DevTree T, int pass, int last, unsigned long long seed, int defer_big) {
   extern __shared__ __align__(16) unsigned char dsm[];
   check_body<D, MODE, XT>(T, pass, last, seed, blockIdx.x, gridDim.x, dsm, defer_big != 0);
 }
