@@ -618,7 +618,7 @@ constexpr long long kDynWaitLimit = 1LL << 24;
 // created and not yet finished; a simplex adds its D + 1 items before its
 // parent item finishes and before it is marked ready, so the count reaches
 // zero only when the region is complete.  rdy[k] marks cavity entry k as
-// stored (rdy: S.maxc ints of the caller's stretch).  Same region, facets
+// stored (rdy: S.maxc ints, in shared memory).  Same region, facets
 // and capacity flags as the wave form; only the order of the lists differs.
 template <int D, int XT>
 __device__ void cavity_search_dyn(const DevTree& T, const CavStore& S, WarpCtl& ctl, int* rdy, int rank,
