@@ -286,12 +286,14 @@ int grow(T** p, int64_t* cap, int64_t want, int64_t keep, int fill, cudaStream_t
   if (want <= *cap) return vd::E_OK;
   T* np = nullptr;
   if (dalloc(&np, (size_t)want) != vd::E_OK) return vd::E_NOMEM;
-  if (*p && keep > 0) cudaMemcpyAsync(np, *p, sizeof(T) * keep, cudaMemcpyDeviceToDevice, st);
-  if (fill >= 0) cudaMemsetAsync(np + keep, fill, sizeof(T) * (want - keep), st);
-  if (*p) {
-    cudaStreamSynchronize(st);
-    cudaFree(*p);
+  if ((*p && keep > 0 &&
+       cudaMemcpyAsync(np, *p, sizeof(T) * keep, cudaMemcpyDeviceToDevice, st) != cudaSuccess) ||
+      (fill >= 0 && cudaMemsetAsync(np + keep, fill, sizeof(T) * (want - keep), st) != cudaSuccess) ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    cudaFree(np);  // the old array and its capacity stay as they were
+    return vd::E_CUDA;
   }
+  if (*p) cudaFree(*p);
   *p = np;
   *cap = want;
   return vd::E_OK;
@@ -343,6 +345,10 @@ int ensure_points(vd_tree* t, int64_t n_new) {
     dfree(t->T.win);
     dfree(t->T.bigc);
     dfree(t->T.bigw);
+    // capacities read as empty until every array is back: a failed
+    // allocation must not leave a later, smaller call on freed arrays
+    t->cap_act = 0;
+    t->T.cap_cand = 0;
     if (dalloc(&t->T.act[0], c) || dalloc(&t->T.act[1], c) || dalloc(&t->T.cand, c) ||
         dalloc(&t->T.cinfo, c) || dalloc(&t->T.wl[0], c) || dalloc(&t->T.wl[1], c) ||
         dalloc(&t->T.order, c) || dalloc(&t->T.win, c) || dalloc(&t->T.bigc, c) || dalloc(&t->T.bigw, c))
@@ -355,6 +361,7 @@ int ensure_points(vd_tree* t, int64_t n_new) {
       0x7fffffffLL);
   if (pool_want > t->T.cap_pool) {
     dfree(t->T.pool);
+    t->T.cap_pool = 0;
     if (dalloc(&t->T.pool, pool_want)) return vd::E_NOMEM;
     t->T.cap_pool = (int)pool_want;
   }
@@ -375,6 +382,8 @@ void drop_graphs(vd_tree* t) {
 }
 
 void release(vd_tree* t) {
+  if (!t) return;
+  if (t->stream) cudaStreamSynchronize(t->stream);
   drop_graphs(t);
   dfree(t->T.sets);
   dfree(t->T.set_of);
@@ -383,8 +392,6 @@ void release(vd_tree* t) {
   dfree(t->d_cr);
   dfree(t->d_flags);
   dfree(t->d_mm);
-  if (!t) return;
-  if (t->stream) cudaStreamSynchronize(t->stream);
   dfree(t->T.pts);
   dfree(t->T.ptf);
   dfree(t->T.simp);
@@ -463,6 +470,7 @@ int ensure_sets(vd_tree* t, int64_t nsets) {
   dfree(t->d_cr);
   dfree(t->d_flags);
   dfree(t->d_mm);
+  t->cap_sets = 0;
   if (dalloc(&t->T.sets, c) || dalloc(&t->d_setoff, c + 1) || dalloc(&t->d_eoff, c + 1) ||
       dalloc(&t->d_cr, 4 * c) || dalloc(&t->d_flags, c) || dalloc(&t->d_mm, 6 * c))
     return vd::E_NOMEM;
@@ -870,6 +878,7 @@ int run_rounds(vd_tree* t, int& r, int64_t n_call, uint64_t seed) {
     if (h.pool_overflow) {
       int64_t want = std::min<int64_t>((int64_t)t->T.cap_pool * 2, 0x7fffffffLL);
       dfree(t->T.pool);
+      t->T.cap_pool = 0;
       if (dalloc(&t->T.pool, want)) {
         rc = vd::E_NOMEM;
         break;
@@ -973,6 +982,7 @@ int ensure_edge_scratch(vd_tree* t, int64_t n_in, int64_t nsimp) {
     dfree(t->es.big);
     dfree(t->es.nbig);
     dfree(t->es.scan_tmp);
+    t->es_n = -1;  // empty until every array is back (see ensure_points)
     const int64_t m = n_in + 2;
     if (dalloc(&t->es.cnt, m) || dalloc(&t->es.off, m) || dalloc(&t->es.ucnt, m) ||
         dalloc(&t->es.uoff, m) || dalloc(&t->es.big, m) || dalloc(&t->es.nbig, 1) ||
@@ -982,11 +992,13 @@ int ensure_edge_scratch(vd_tree* t, int64_t n_in, int64_t nsimp) {
   }
   if (t->es.cap_buf < buf_want) {
     dfree(t->es.buf);
+    t->es.cap_buf = 0;
     if (dalloc(&t->es.buf, buf_want)) return vd::E_NOMEM;
     t->es.cap_buf = buf_want;
   }
   if (t->cap_edges < buf_want) {
     dfree(t->d_edges);
+    t->cap_edges = 0;
     if (dalloc(&t->d_edges, buf_want)) return vd::E_NOMEM;
     t->cap_edges = buf_want;
   }
@@ -1213,6 +1225,7 @@ int vd_delaunay_tree(vd_tree* t, const double* pts, int64_t n, uint64_t seed, ui
   if (!t || !t->hctr || !pts || n < 1) return VD_ERR_ARG;
   if (n * t->dim > t->cap_in) {
     dfree(t->d_in);
+    t->cap_in = 0;
     if (dalloc(&t->d_in, (size_t)(n * t->dim))) return VD_ERR_NOMEM;
     t->cap_in = n * t->dim;
   }
