@@ -575,20 +575,22 @@ VDP_HD int insphere_int(const VPt* p, const VPt& q, int* s) {
 
 // Exact, perturbed insphere (3D) / incircle (2D).  p[i] positively oriented.
 // With sos = false the plain sign of the lifted determinant is returned
-// (0 when q is exactly on the circumsphere).
+// (0 when q is exactly on the circumsphere).  `tie`, when given, is set to 1
+// if the answer came from the symbolic perturbation (an exact tie).
 //
 // XT selects the integer tier in front of the expansions.  The integer code
 // is wide (many live limbs); a kernel whose register allocation must stay
 // small calls the XT = 0 form, which is the expansion path alone.
 template <int D, int XT = 1>
 VDP_NI int exact_insphere_sos(const VPt* p, const int* key, const VPt& q, int qkey, int& err,
-                              bool sos = true) {
+                              bool sos = true, int* tie = nullptr) {
   constexpr int NV = D + 1;
   if constexpr (XT != 0) {
     int si[NV];
     const int r = insphere_int<D>(p, q, si);
     if (r != 2) {
       if (r != 0 || !sos) return r;
+      if (tie) *tie = 1;
       return sos_decide<NV>(si, key, qkey);
     }
   }
@@ -624,6 +626,7 @@ VDP_NI int exact_insphere_sos(const VPt* p, const int* key, const VPt& q, int qk
   }
   int sg = xp_sign(det);
   if (sg != 0 || !sos) return sg;
+  if (tie) *tie = 1;
   return sos_decide<NV>(s, key, qkey);
 }
 
@@ -735,7 +738,9 @@ VDP_HD bool in_conflict(const VPt* p, const int* key, const VPt& q, int qkey, Ta
     return s > 0;
   }
   t.exact++;
-  s = exact_insphere_sos<D>(p, key, q, qkey, err);
+  int tie = 0;
+  s = exact_insphere_sos<D>(p, key, q, qkey, err, true, &tie);
+  t.sos += tie;
   return s > 0;
 }
 
@@ -1033,7 +1038,9 @@ VDP_HD bool in_conflict_64(const VPt* p, const int* key, const VPt& q, int qkey,
     return s > 0;
   }
   t.exact++;
-  s = exact_insphere_sos<D, XT>(p, key, q, qkey, err);
+  int tie = 0;
+  s = exact_insphere_sos<D, XT>(p, key, q, qkey, err, true, &tie);
+  t.sos += tie;
   return s > 0;
 }
 
