@@ -246,6 +246,17 @@ int vd_set_early_phase(vd_tree* t, int64_t until_inserted, int thin, double rati
  * reference's conflict test (circumsphere centre and radius, then a distance
  * comparison in f64, src/geometry.rs:58-97) has no exact tier. */
 int vd_set_exact_tier(vd_tree* t, int mode, int64_t switch_after);
+/* First points of a fresh single-set call (no reference counterpart; the
+ * reference inserts the first 1e5 points one at a time, src/lib.rs:108-114).
+ * While the triangulation is small, a device-wide round inserts only one or a
+ * few points, so the first whole priority levels, at most `max_points` points
+ * and at most the block's capacity (320 in 3D, 640 in 2D), are inserted one
+ * after another by one thread block holding the triangulation in shared
+ * memory; the rounds continue from there.  The triangulation is the same.
+ * Default: 150 points (the block's time per point grows with the
+ * triangulation, so past a few hundred points the rounds are faster); 0
+ * turns it off. */
+int vd_set_first_block(vd_tree* t, int64_t max_points);
 /* Rounds are launched in chunks captured once as CUDA graphs and replayed
  * (default on; profiling and tracing launch kernel by kernel).  No reference
  * counterpart. */

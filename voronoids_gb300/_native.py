@@ -27,7 +27,7 @@ EXPORTS = [
     "vd_edges_device", "vd_check_delaunay", "vd_duplicates", "vd_get_stats", "vd_status_str",
     "vd_delaunay", "vd_set_schedule", "vd_set_tuning", "vd_set_graphs", "vd_set_profiling", "vd_profile", "vd_profile_name", "vd_set_trace", "vd_trace", "vd_kernel_launches", "vd_edges_from_simplices_noalloc",
     "vd_batch_delaunay", "vd_batch_delaunay_device", "vd_num_sets", "vd_tree_create",
-    "vd_set_launch", "vd_autotune_batch", "vd_locate_points", "vd_set_adjacent", "vd_circumspheres", "vd_set_small_rounds", "vd_set_early_phase", "vd_set_exact_tier",
+    "vd_set_launch", "vd_autotune_batch", "vd_locate_points", "vd_set_adjacent", "vd_circumspheres", "vd_set_small_rounds", "vd_set_early_phase", "vd_set_exact_tier", "vd_set_first_block",
     "vd_server_new", "vd_server_submit", "vd_server_poll", "vd_server_result", "vd_server_stats", "vd_server_free",
     "vd_check_triangulation", "vd_voronoi_edges", "vd_voronoi_cells",
 ]
@@ -100,6 +100,7 @@ def load(path=LIB_PATH):
         "vd_set_adjacent": ([vp, ctypes.c_int], ctypes.c_int),
         "vd_set_small_rounds": ([vp, ctypes.c_int], ctypes.c_int),
         "vd_set_early_phase": ([vp, i64, ctypes.c_int, ctypes.c_double], ctypes.c_int),
+        "vd_set_first_block": ([vp, i64], ctypes.c_int),
         "vd_set_exact_tier": ([vp, ctypes.c_int, i64], ctypes.c_int),
         "vd_circumspheres": ([vp, dp, dp, i64, i64p], ctypes.c_int),
         "vd_locate_points": ([vp, dp, i64, i64p, i64p, i64], ctypes.c_int),

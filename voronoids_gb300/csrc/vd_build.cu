@@ -2173,6 +2173,369 @@ __global__ void __launch_bounds__(32) k_insert_one(DevTree T, double x, double y
   }
 }
 
+// ---------------------------------------------------------------------------
+// The first points of a fresh single-set build, one after another in one
+// block, with the whole triangulation in shared memory.
+//
+// While the triangulation is small, nearly every conflict region holds part of
+// the super simplex's star, so a device-wide round inserts one or a few points
+// for about ten dependent kernel launches.  Here one 512-thread block inserts
+// the first priority levels (Bowyer-Watson in the reference's sense,
+// src/delaunay_tree.rs:125-211, one point at a time):
+//   1. every live simplex is tested against the point (exact, perturbed
+//      conflict test keyed by the global vertex ids, as in the rounds), so no
+//      point location is needed;
+//   2. the faces of the conflict region whose neighbour is outside it are the
+//      boundary facets; no conflict region means the point duplicates a vertex;
+//   3. each facet gets a new simplex (a region slot first, then a fresh slot)
+//      with its outer link, and the faces through the new point are paired
+//      through a ridge table.
+// The triangulation is unique, so any insertion order gives the one the
+// rounds would build.  The tree in global memory is written only at the end,
+// compacted (live simplices in slots 0..m-1) with the location hints of every
+// point; when any capacity below would be exceeded the kernel writes nothing
+// and the rounds insert these points as usual.
+constexpr int kSeedThreads = 512;
+template <int D>
+struct SeedCap;
+template <>
+struct SeedCap<3> {
+  static constexpr int S = 2560, P = 324, C = 1024, F = 1024, H = 4096, DUP = 64;
+};
+template <>
+struct SeedCap<2> {
+  static constexpr int S = 2560, P = 644, C = 1024, F = 1024, H = 4096, DUP = 64;
+};
+// Shared-memory layout of k_seed (bytes), in this order: simplex vertices and
+// neighbour codes (local ids), point records and global ids, cavity marks,
+// cavity, facets (new vertices, outer code, position of the new point), ridge
+// table (keys, first and second half), flags of inserted points, duplicates.
+template <int D>
+constexpr size_t seed_smem() {
+  using C = SeedCap<D>;
+  return (size_t)C::S * 32 + (size_t)C::P * (sizeof(vdp::FPt) + 4) + (size_t)C::S * 4 + (size_t)C::C * 4 +
+         (size_t)C::F * 24 + (size_t)C::H * 16 + (size_t)C::P * 4 + (size_t)C::DUP * 8;
+}
+__device__ __forceinline__ unsigned seed_hash(int r0, int r1, int H) {
+  return ((((unsigned)r0 * 0x9E3779B1u) ^ ((unsigned)r1 * 0x85EBCA77u)) >> 12) & (unsigned)(H - 1);
+}
+// Slot of the key (epoch, r0, r1) in the ridge table, -1 if absent.
+__device__ __forceinline__ int seed_find(const unsigned long long* hk, int H, unsigned long long key, int r0, int r1) {
+  unsigned h = seed_hash(r0, r1, H);
+  for (int probe = 0; probe < H; ++probe, h = (h + 1) & (unsigned)(H - 1)) {
+    const unsigned long long k = hk[h];
+    if (k == key) return (int)h;
+    if ((k >> 32) != (key >> 32)) return -1;  // an entry of an earlier point: the key is not there
+  }
+  return -1;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kSeedThreads, 1) k_seed(DevTree T, int npts, int nlev, unsigned long long seed) {
+  using C = SeedCap<D>;
+  constexpr int NV = D + 1;
+  extern __shared__ __align__(16) unsigned char seed_sm[];
+  int4* sv = reinterpret_cast<int4*>(seed_sm);
+  int4* sn = sv + C::S;
+  vdp::FPt* fp = reinterpret_cast<vdp::FPt*>(sn + C::S);
+  int* gid = reinterpret_cast<int*>(fp + C::P);
+  int* mark = gid + C::P;
+  int* cav = mark + C::S;
+  int4* fnv = reinterpret_cast<int4*>(cav + C::C);
+  int* fcode = reinterpret_cast<int*>(fnv + C::F);
+  int* fqf = fcode + C::F;
+  unsigned long long* hk = reinterpret_cast<unsigned long long*>(fqf + C::F);
+  int* ha = reinterpret_cast<int*>(hk + C::H);
+  int* hb = ha + C::H;
+  int* ins = hb + C::H;
+  int2* dl = reinterpret_cast<int2*>(ins + C::P);
+  __shared__ int s_ns, s_ncav, s_nfac, s_abort, s_ndup, s_dupof, s_nins;
+  __shared__ unsigned long long s_created, s_killed;
+  __shared__ int s_maxc, s_maxf, s_holes;
+  const int tid = threadIdx.x;
+  const SetGeo& g = T.sets[0];
+  if (T.nsets != 1 || npts < 1 || npts + NV > C::P || npts > C::C || npts > C::S) return;
+  // start: the super simplex (local vertices 0..D) and the points of the
+  // levels in priority order (local vertex NV + k is the k-th lowest), so that
+  // of equal points the one with the lowest priority is inserted and the
+  // others are its duplicates, as in the rounds
+  for (int i = tid; i < npts; i += kSeedThreads) {
+    const int v = T.order[i];
+    mark[i] = v;
+    cav[i] = (int)priority((uint32_t)v, seed);
+  }
+  for (int i = tid; i < C::H; i += kSeedThreads) hk[i] = 0ull;
+  __syncthreads();
+  for (int i = tid; i < npts; i += kSeedThreads) {
+    const unsigned pr = (unsigned)cav[i];
+    int rank = 0;
+    for (int j = 0; j < npts; ++j) rank += (unsigned)cav[j] < pr ? 1 : 0;
+    const int v = mark[i];
+    const bool bad = bad_vert(T, v);
+    if (bad) set_error(T.ctr, E_INTERNAL);
+    gid[NV + rank] = bad ? 0 : v;
+    fp[NV + rank] = load_fpt(T, bad ? 0 : v);
+    ins[NV + rank] = 0;
+  }
+  for (int l = tid; l < NV; l += kSeedThreads) {
+    const int v = g.sup[l];
+    const bool bad = bad_vert(T, v);
+    if (bad) set_error(T.ctr, E_INTERNAL);
+    gid[l] = bad ? 0 : v;
+    fp[l] = load_fpt(T, bad ? 0 : v);
+    ins[l] = 1;
+  }
+  __syncthreads();
+  for (int i = tid; i < C::S; i += kSeedThreads) mark[i] = 0;
+  if (tid == 0) {
+    sv[0] = D == 3 ? make_int4(0, 1, 2, 3) : make_int4(0, 1, 2, -1);
+    sn[0] = make_int4(-1, -1, -1, -1);
+    s_ns = 1;
+    s_ncav = s_nfac = s_abort = s_ndup = s_nins = 0;
+    s_created = s_killed = 0ull;
+    s_maxc = s_maxf = s_holes = 0;
+  }
+  __syncthreads();
+  vdp::Tally tl = {0, 0, 0, 0};
+  int perr = 0;
+  unsigned ntests = 0;
+  for (int p = 0; p < npts; ++p) {
+    const int ql = NV + p, qv = gid[ql];
+    const vdp::FPt fq = fp[ql];
+    const int ns = s_ns;
+    // 0. a point equal to an inserted vertex is skipped and recorded, as the
+    // rounds do before any search (its conflict region need not be empty:
+    // the perturbation of an equal vertex with a larger id puts it inside)
+    if (tid == 0) s_dupof = -1;
+    __syncthreads();
+    for (int l = tid; l < ql; l += kSeedThreads) {
+      if (!ins[l]) continue;
+      const vdp::FPt& a = fp[l];
+      if (a.hx == fq.hx && a.hy == fq.hy && a.hz == fq.hz && a.lx == fq.lx && a.ly == fq.ly && a.lz == fq.lz &&
+          same_point_bits(load_pt(T, gid[l]), load_pt(T, qv)))
+        s_dupof = gid[l];
+    }
+    __syncthreads();
+    if (s_dupof >= 0) {
+      if (tid == 0) {
+        if (s_ndup >= C::DUP) s_abort = 1;
+        else dl[s_ndup++] = make_int2(qv, s_dupof);
+      }
+      __syncthreads();
+      if (s_abort) break;
+      continue;
+    }
+    // 1. conflict region: every live simplex, exact perturbed test
+    for (int s = tid; s < ns; s += kSeedThreads) {
+      const int4 v = sv[s];
+      if (v.x < 0) continue;
+      vdp::FPt fv[NV];
+      int kv[NV];
+      for (int j = 0; j < NV; ++j) {
+        const int l = get4(v, j);
+        kv[j] = gid[l];
+        fv[j] = fp[l];
+      }
+      ++ntests;
+      auto load64 = [&](vdp::VPt* v64, vdp::VPt& q64) {
+        for (int j = 0; j < NV; ++j) v64[j] = load_pt(T, kv[j]);
+        q64 = load_pt(T, qv);
+      };
+      if (vdp::in_conflict_hl<D, 1>(fv, kv, fq, qv, tl, perr, load64)) {
+        const int k = atomicAdd(&s_ncav, 1);
+        if (k < C::C) cav[k] = s;
+        mark[s] = p + 1;
+      }
+    }
+    __syncthreads();
+    const int ncav = s_ncav;
+    if (ncav > C::C) break;  // s_abort is set below, by thread 0
+    if (ncav == 0) {
+      // a point that is no vertex lies in the closed simplex that contains
+      // it, and so inside its circumsphere: an empty region is a fault
+      if (tid == 0) {
+        set_error(T.ctr, E_INTERNAL);
+        s_abort = 1;
+      }
+      __syncthreads();
+      break;
+    }
+    // 2. boundary facets: faces of the region whose neighbour is outside it
+    // (the ridge table's halves are emptied meanwhile)
+    for (int i = tid; i < C::H; i += kSeedThreads) {
+      ha[i] = -1;
+      hb[i] = -1;
+    }
+    for (int it = tid; it < ncav * NV; it += kSeedThreads) {
+      const int k = it / NV, f = it - k * NV;
+      const int s = cav[k];
+      const int code = get4(sn[s], f);
+      if (code >= 0 && mark[code >> 2] == p + 1) continue;
+      const int j = atomicAdd(&s_nfac, 1);
+      if (j < C::F) {
+        fnv[j] = set4(sv[s], f, ql);
+        fcode[j] = code;
+        fqf[j] = f;
+      }
+    }
+    __syncthreads();
+    const int nfac = s_nfac;
+    if (nfac > C::F || ns + max(0, nfac - ncav) > C::S) break;
+    // 3a. ridge table: each face through the new point, keyed by its other
+    // old vertices (3D: two, 2D: one), takes the first or the second half
+    const unsigned long long ep = (unsigned long long)(p + 1) << 32;
+    for (int it = tid; it < nfac * NV; it += kSeedThreads) {
+      const int j = it / NV, gf = it - j * NV, qf = fqf[j];
+      if (gf == qf) continue;
+      int r[4] = {fnv[j].x, fnv[j].y, fnv[j].z, fnv[j].w};
+      int r0, r1;
+      ridge_of<D>(r, gf, qf, r0, r1);
+      const unsigned long long key = ep | ((unsigned long long)(unsigned)(r0 & 0xffff) << 16) | (unsigned)(r1 & 0xffff);
+      unsigned h = seed_hash(r0, r1, C::H);
+      for (int probe = 0; probe < C::H; ++probe, h = (h + 1) & (unsigned)(C::H - 1)) {
+        unsigned long long cur = hk[h];
+        if ((cur >> 32) != (unsigned long long)(p + 1)) {
+          const unsigned long long old = atomicCAS(&hk[h], cur, key);
+          if (old == cur) {
+            ha[h] = (j << 2) | gf;
+            break;
+          }
+          cur = old;
+        }
+        if (cur == key) {
+          hb[h] = (j << 2) | gf;
+          break;
+        }
+      }
+    }
+    __syncthreads();
+    // 3b. new simplices: facet j takes region slot cav[j], or a fresh slot
+    for (int j = tid; j < nfac; j += kSeedThreads) {
+      const int slot = j < ncav ? cav[j] : ns + (j - ncav);
+      const int qf = fqf[j];
+      const int4 nv = fnv[j];
+      int r[4] = {nv.x, nv.y, nv.z, nv.w};
+      int4 nn = make_int4(-1, -1, -1, -1);
+      for (int gf = 0; gf < NV; ++gf) {
+        if (gf == qf) {
+          nn = set4(nn, gf, fcode[j]);
+          continue;
+        }
+        int r0, r1;
+        ridge_of<D>(r, gf, qf, r0, r1);
+        const unsigned long long key = ep | ((unsigned long long)(unsigned)(r0 & 0xffff) << 16) | (unsigned)(r1 & 0xffff);
+        const int h = seed_find(hk, C::H, key, r0, r1);
+        const int mine = (j << 2) | gf;
+        const int other = h < 0 ? -1 : (ha[h] == mine ? hb[h] : ha[h]);
+        if (other < 0 || (other >> 2) >= nfac) {
+          set_error(T.ctr, E_INTERNAL);  // a ridge with one half: not a closed star
+          s_abort = 1;
+          continue;
+        }
+        const int oj = other >> 2;
+        const int oslot = oj < ncav ? cav[oj] : ns + (oj - ncav);
+        nn = set4(nn, gf, (oslot << 2) | (other & 3));
+      }
+      sv[slot] = nv;
+      sn[slot] = nn;
+    }
+    __syncthreads();
+    // 3c. outer neighbours point at the new simplices; region slots without a
+    // facet die (their records are not read again)
+    for (int j = tid; j < nfac; j += kSeedThreads) {
+      const int code = fcode[j];
+      if (code < 0) continue;
+      const int slot = j < ncav ? cav[j] : ns + (j - ncav);
+      reinterpret_cast<int*>(sn + (code >> 2))[code & 3] = (slot << 2) | fqf[j];
+    }
+    for (int k = nfac + tid; k < ncav; k += kSeedThreads) sv[cav[k]].x = -1;
+    __syncthreads();
+    if (tid == 0) {
+      s_ns = ns + max(0, nfac - ncav);
+      s_ncav = 0;
+      s_nfac = 0;
+      s_nins += 1;
+      s_created += nfac;
+      s_killed += ncav;
+      s_maxc = max(s_maxc, ncav);
+      s_maxf = max(s_maxf, nfac);
+      s_holes += max(0, ncav - nfac);
+      ins[ql] = 1;
+    }
+    __syncthreads();
+    if (s_abort) break;
+  }
+  // a loop left early (capacity) has not finished its point
+  if (tid == 0 && (s_ncav > C::C || s_nfac > C::F || s_ncav != 0 || s_nfac != 0)) s_abort = 1;
+  __syncthreads();
+  if (perr) set_error(T.ctr, E_PRECISION);
+  if (s_abort) return;  // nothing written: the rounds insert these points
+  // write-out: live slots are ranked (mark[] holds the ranks) and stored
+  // compacted with global vertex ids and neighbour codes
+  const int ns = s_ns;
+  __shared__ int wsum[kSeedThreads / 32];
+  constexpr int PER = (C::S + kSeedThreads - 1) / kSeedThreads;
+  int cnt = 0;
+  for (int k = 0; k < PER; ++k) {
+    const int s = tid * PER + k;
+    cnt += (s < ns && sv[s].x >= 0) ? 1 : 0;
+  }
+  int incl = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(FULL, incl, o);
+    if ((tid & 31) >= o) incl += y;
+  }
+  if ((tid & 31) == 31) wsum[tid >> 5] = incl;
+  __syncthreads();
+  int base = 0;
+  for (int w = 0; w < (tid >> 5); ++w) base += wsum[w];
+  base += incl - cnt;
+  for (int k = 0; k < PER; ++k) {
+    const int s = tid * PER + k;
+    if (s < ns && sv[s].x >= 0) mark[s] = base++;
+  }
+  __syncthreads();
+  int nlive = 0;
+  for (int w = 0; w < kSeedThreads / 32; ++w) nlive += wsum[w];
+  if (nlive > T.cap_simp) {
+    if (tid == 0) set_error(T.ctr, E_INTERNAL);
+    return;
+  }
+  for (int s = tid; s < ns; s += kSeedThreads) {
+    const int4 v = sv[s];
+    if (v.x < 0) continue;
+    const int4 n = sn[s];
+    int4 gv = make_int4(-1, -1, -1, -1), gn = make_int4(-1, -1, -1, -1);
+    for (int j = 0; j < NV; ++j) {
+      gv = set4(gv, j, gid[get4(v, j)]);
+      const int c = get4(n, j);
+      gn = set4(gn, j, c < 0 ? -1 : (mark[c >> 2] << 2) | (c & 3));
+    }
+    store_simplex(T, mark[s], gv, gn);
+    for (int j = 0; j < NV; ++j) {
+      const int l = get4(v, j);
+      if (l >= NV) write_hints<D>(T, gid[l], fp[l], mark[s]);
+    }
+  }
+  flush_tally(T.ctr, tl, ntests, 0);
+  if (tid == 0) {
+    Counters* c = T.ctr;
+    c->nsimp = nlive;
+    c->ninserted += s_nins;
+    c->winners += s_nins;
+    c->created += s_created;
+    c->killed += s_killed;
+    c->holes += s_holes;
+    c->max_cav = max(c->max_cav, s_maxc);
+    c->max_fac = max(c->max_fac, s_maxf);
+    const int d0 = c->ndup;
+    for (int k = 0; k < s_ndup; ++k)
+      if (d0 + k < T.cap_dups) T.dups[d0 + k] = dl[k];
+    c->ndup = d0 + s_ndup;
+    c->lev_next = nlev;
+  }
+}
+
 template <int D>
 constexpr size_t small_rounds_smem() {
   return 4 * sizeof(WarpCav<D>) > 4 * sizeof(WarpCommit<D>) ? 4 * sizeof(WarpCav<D>) : 4 * sizeof(WarpCommit<D>);
@@ -2310,6 +2673,8 @@ int prepare_once() {
   attr((const void*)k_cavity_big<3, 1>, kBigSmem);
   attr((const void*)k_cavity_big<2, 0>, kBigSmem);
   attr((const void*)k_cavity_big<2, 1>, kBigSmem);
+  attr((const void*)k_seed<3>, (int)seed_smem<3>());
+  attr((const void*)k_seed<2>, (int)seed_smem<2>());
   if (e != cudaSuccess) return E_CUDA;
   // k_check is a grid-stride loop: one resident wave avoids a ragged second
   int dev = 0, sms = 0, b3 = 0, b2 = 0, c3 = 0, c2 = 0;
@@ -2386,6 +2751,16 @@ int launch_small_rounds(const DevTree& T, cudaStream_t stream, int dim, const Tu
   return E_OK;
 }
 
+int seed_max_points(int dim) { return dim == 3 ? SeedCap<3>::P - 4 : SeedCap<2>::P - 3; }
+
+void launch_seed(const DevTree& T, cudaStream_t stream, int dim, int npts, int nlev, uint64_t seed) {
+  note_launches(1);
+  if (dim == 3)
+    k_seed<3><<<1, kSeedThreads, seed_smem<3>(), stream>>>(T, npts, nlev, seed);
+  else
+    k_seed<2><<<1, kSeedThreads, seed_smem<2>(), stream>>>(T, npts, nlev, seed);
+}
+
 void launch_insert_one(const DevTree& T, cudaStream_t stream, int dim, const double* c, int vid) {
   note_launches(1);
   if (dim == 3)
@@ -2403,6 +2778,7 @@ void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, 
 
 const char* const kKernelTypeNames[KT_COUNT] = {"k_pick",     "k_thin",         "k_cavity",     "k_check",
                                                 "k_reclaim",  "k_relocate",     "k_activate",   "edges",
-                                                "k_decide",   "k_rounds_small", "k_cavity_big", "k_commit_big"};
+                                                "k_decide",   "k_rounds_small", "k_cavity_big", "k_commit_big",
+                                                "k_seed"};
 
 }  // namespace vd

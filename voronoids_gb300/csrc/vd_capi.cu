@@ -207,6 +207,10 @@ struct vd_tree {
   // 1 expansions only, 2 integer tier first from the start
   int exact_mode = 0;
   int64_t exact_switch = 32;
+  // most points a fresh single-set call inserts in one block before its
+  // rounds (whole priority levels, up to the block's capacity; 0: none; -1:
+  // the dimension's default, 150 points in 2D and 3D)
+  int64_t first_block = -1;
 };
 
 namespace {
@@ -944,11 +948,31 @@ int insert_device(vd_tree* t, const double* d_xyz, int64_t n, uint64_t seed) {
   }
   cudaMemsetAsync(t->d_counts, 0, sizeof(int) * 2 * vd::kMaxLevels, t->stream);
   vd::launch_levels(t->T, L, n, base, seed, thr.data(), (int)thr.size(), first, t->growth, t->d_counts);
+  // a fresh single-set call starts with its first levels in one block
+  const int64_t fb_max = t->first_block >= 0 ? t->first_block : 150;
+  const bool first_block = fb_max > 0 && t->nsets == 1 && t->hctr->ninserted == 0 && t->hctr->ndup == 0;
+  std::vector<int> lev_counts(thr.size(), 0);
+  if (first_block)
+    cudaMemcpyAsync(lev_counts.data(), t->d_counts, sizeof(int) * lev_counts.size(), cudaMemcpyDeviceToHost,
+                    t->stream);
   rc = sync_counters(t);
   if (rc) return rc;
   if (t->hctr->err) return t->hctr->err;
   t->nverts += n;
   t->calls++;
+  if (first_block) {
+    const int64_t cap = std::min<int64_t>(fb_max, vd::seed_max_points(t->dim));
+    int64_t pts = 0;
+    int levs = 0;
+    for (size_t k = 0; k < lev_counts.size() && pts + lev_counts[k] <= cap; ++k) {
+      pts += lev_counts[k];
+      levs = (int)k + 1;
+    }
+    if (levs > 0 && pts > 0) {
+      ScopedProf sp(t, vd::KT_SEED);
+      vd::launch_seed(t->T, t->stream, t->dim, (int)pts, levs, seed);
+    }
+  }
   int r = t->round;
   rc = run_rounds(t, r, n, seed);
   t->round = r;
@@ -1521,6 +1545,12 @@ int vd_set_early_phase(vd_tree* t, int64_t until_inserted, int thin, double rati
   t->early_until = until_inserted;
   t->early_thin = thin;
   t->early_ratio = ratio;
+  return VD_OK;
+}
+
+int vd_set_first_block(vd_tree* t, int64_t max_points) {
+  if (ready(t) || max_points < 0) return VD_ERR_ARG;
+  t->first_block = max_points;
   return VD_OK;
 }
 

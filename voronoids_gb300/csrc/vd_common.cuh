@@ -283,6 +283,7 @@ enum {
   KT_SMALL,
   KT_BIG,
   KT_BIGW,
+  KT_SEED,
   KT_COUNT
 };
 extern const char* const kKernelTypeNames[KT_COUNT];
@@ -305,6 +306,14 @@ void launch_round(const DevTree& T, const Launch& L, int dim, const Tuning& tu, 
 // its vertex id vid (the next one of the tree).  ctr->single receives the
 // outcome (see k_insert_one in vd_build.cu).
 void launch_insert_one(const DevTree& T, cudaStream_t stream, int dim, const double* c, int vid);
+// The first `npts` points of `order` (the first `nlev` priority levels of a
+// fresh single-set call, priorities under `seed`) inserted one after another
+// by one block, the triangulation in shared memory (k_seed in vd_build.cu).
+// On success the tree holds them, compacted, with their hints, and the level
+// feed starts at level nlev; if a shared-memory capacity would be exceeded
+// nothing is written and the rounds insert them.  npts <= seed_max_points(dim).
+void launch_seed(const DevTree& T, cudaStream_t stream, int dim, int npts, int nlev, uint64_t seed);
+int seed_max_points(int dim);
 // Rounds while few points are active, in one cooperative launch (all blocks
 // resident, grid barrier between phases): runs until the next round's active
 // set reaches `max_active`, the call is done, `max_rounds` rounds ran, a pool

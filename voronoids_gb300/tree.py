@@ -325,6 +325,12 @@ class DelaunayTree:
         _check(_native.load().vd_set_early_phase(self._h, int(until_inserted), int(thin), float(ratio)),
                "set_early_phase")
 
+    def set_first_block(self, max_points):
+        """First whole priority levels of a fresh call (at most ``max_points``, capped by the
+        block's capacity of 320 points in 3D and 640 in 2D) inserted by one block before the
+        rounds; 0 turns it off (default: 150)."""
+        _check(_native.load().vd_set_first_block(self._h, int(max_points)), "set_first_block")
+
     def set_exact_tier(self, mode=0, switch_after=32):
         """Exact tier of the conflict tests: 0 automatic, 1 expansions only, 2 integer first (see vd_set_exact_tier)."""
         _check(_native.load().vd_set_exact_tier(self._h, int(mode), int(switch_after)), "set_exact_tier")
