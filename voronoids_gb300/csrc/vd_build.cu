@@ -1754,7 +1754,9 @@ __device__ __forceinline__ void fix_body(DevTree T, int bid, int nblk) {
   const int nw = nblk * (blockDim.x >> 5);
   const int n = T.ctr->nwin;
   const long long nrepl = 4LL * T.cap_simp;
-  for (int it = bid * (blockDim.x >> 5) + wib; it < n; it += nw) {
+  // the last warps of the grid take the winners, so that in a small round the
+  // first warps, which relocate the points, do not wait for this chain first
+  for (int it = nw - 1 - (bid * (blockDim.x >> 5) + wib); it < n; it += nw) {
     const int c = T.win[it];
     const int4 info = T.cinfo[c];
     if (info.w != ST_DONE) continue;
