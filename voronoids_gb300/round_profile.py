@@ -13,7 +13,10 @@ build's counterpart:
 * ``rounds``: one traced build (kernel by kernel, one synchronisation per
   round), summed by the number of active points at the start of a round.
 
-    python -m voronoids_gb300.round_profile [--dim 3] [--n 1000000]
+    python -m voronoids_gb300.round_profile [--dim 3] [--n 1000000] [--first-block N]
+
+``--first-block`` sets how many first points one block inserts before the
+rounds (``vd_set_first_block``; 0: none, default: the library's).
 """
 import argparse
 import ctypes
@@ -25,7 +28,7 @@ from . import _native
 from . import workloads as W
 
 
-def _tree_on_device(L, torch, pts):
+def _tree_on_device(L, torch, pts, first_block=None):
     n, dim = pts.shape
     dev = torch.from_numpy(np.ascontiguousarray(pts)).cuda().contiguous()
     stream = torch.cuda.current_stream()
@@ -34,7 +37,10 @@ def _tree_on_device(L, torch, pts):
                              ctypes.byref(st))
     if not h or st.value != 0:
         raise RuntimeError(f"vd_tree_new_device failed: {st.value}")
-    return ctypes.c_void_p(h), dev, stream
+    h = ctypes.c_void_p(h)
+    if first_block is not None and L.vd_set_first_block(h, int(first_block)) != 0:
+        raise RuntimeError("vd_set_first_block failed")
+    return h, dev, stream
 
 
 def _profile(L, tree):
@@ -47,7 +53,7 @@ def _profile(L, tree):
     return {L.vd_profile_name(i).decode(): (float(ms[i]), int(cnt[i])) for i in range(nk.value) if cnt[i]}
 
 
-def prefixes(pts, sizes, seed=0x5EED, reps=5):
+def prefixes(pts, sizes, seed=0x5EED, reps=5, first_block=None):
     """One record per prefix size: build time (ms), rounds, microseconds per
     round and per kernel launch."""
     import torch
@@ -55,7 +61,7 @@ def prefixes(pts, sizes, seed=0x5EED, reps=5):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     out = []
     for n in sizes:
-        tree, dev, stream = _tree_on_device(L, torch, pts[:n])
+        tree, dev, stream = _tree_on_device(L, torch, pts[:n], first_block)
         cap = 8 * n + 1024
         uv = torch.empty(2 * cap, dtype=torch.int32, device="cuda")
         m = ctypes.c_int64(0)
@@ -92,7 +98,7 @@ def prefixes(pts, sizes, seed=0x5EED, reps=5):
     return out
 
 
-def rounds(pts, seed=0x5EED, buckets=(0, 1000, 10000, 50000)):
+def rounds(pts, seed=0x5EED, buckets=(0, 1000, 10000, 50000), first_block=None):
     """A traced build summed by active points at the start of a round:
     rounds, GPU milliseconds (per-kernel events, no graphs), points inserted."""
     from .tree import DelaunayTree
@@ -100,6 +106,8 @@ def rounds(pts, seed=0x5EED, buckets=(0, 1000, 10000, 50000)):
     warm.add_points_to_tree(pts, seed=seed)
     warm.close()
     t = DelaunayTree(pts)
+    if first_block is not None:
+        t.set_first_block(first_block)
     t.set_profiling(True)
     t.set_trace(True)
     t.add_points_to_tree(pts, seed=seed)
@@ -120,12 +128,13 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--dim", type=int, default=3, choices=(2, 3))
     ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--first-block", type=int, default=None)
     a = ap.parse_args()
     pts = W.uniform_points(a.n, a.dim, W.config_seed(2 if a.dim == 3 else 1))
     sizes = [s for s in (300, 3000, 30000, 300000) if s < a.n] + [a.n]
-    for rec in prefixes(pts, sizes):
+    for rec in prefixes(pts, sizes, first_block=a.first_block):
         print(json.dumps({"prefix": rec}), flush=True)
-    for rec in rounds(pts):
+    for rec in rounds(pts, first_block=a.first_block):
         print(json.dumps({"rounds_by_active": rec}), flush=True)
 
 
