@@ -250,7 +250,7 @@ int vd_set_exact_tier(vd_tree* t, int mode, int64_t switch_after);
  * reference inserts the first 1e5 points one at a time, src/lib.rs:108-114).
  * While the triangulation is small, a device-wide round inserts only one or a
  * few points, so the first whole priority levels, at most `max_points` points
- * and at most the block's capacity (320 in 3D, 640 in 2D), are inserted one
+ * and at most the block's capacity (320 in 3D, 641 in 2D), are inserted one
  * after another by one thread block holding the triangulation in shared
  * memory; the rounds continue from there.  The triangulation is the same.
  * Default: 150 points (the block's time per point grows with the

@@ -327,7 +327,7 @@ class DelaunayTree:
 
     def set_first_block(self, max_points):
         """First whole priority levels of a fresh call (at most ``max_points``, capped by the
-        block's capacity of 320 points in 3D and 640 in 2D) inserted by one block before the
+        block's capacity of 320 points in 3D and 641 in 2D) inserted by one block before the
         rounds; 0 turns it off (default: 150)."""
         _check(_native.load().vd_set_first_block(self._h, int(max_points)), "set_first_block")
 
