@@ -197,3 +197,43 @@ def test_float_semantics_agree_with_exact_on_uniform_points(oracle):
         res = oracle.validate(p.shape[1], verts, simp, nbr, expect_vertices=len(verts))
         assert bad == 0 and res["asymmetric"] == 0 and res["not_delaunay"] == 0
 
+
+
+def _shells(dim):
+    """The origin and the integer points on concentric spheres (3D) or
+    circles (2D): each shell is exactly cospherical (cocircular)."""
+    out = [np.zeros((1, dim))]
+    for R2 in ((441, 2025) if dim == 3 else (5525, 27625, 71825)):
+        R = int(math.isqrt(R2)) + 1
+        r = np.arange(-R, R + 1)
+        g = np.meshgrid(*([r] * dim), indexing="ij")
+        m = sum(x * x for x in g) == R2
+        out.append(np.stack([x[m] for x in g], 1))
+    return np.concatenate(out).astype(np.float64)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_power_of_two_scaling_keeps_edges(oracle, dim):
+    # rescaling by 2^k is exact, and so is the reference's super simplex of the
+    # rescaled points: the same triangulation, the same edges
+    p = W.uniform_points(600, dim, 870 + dim)
+    want = oracle.Triangulation(p, seed=1).edges()
+    for k in (-100, -30, 30, 100):
+        assert np.array_equal(oracle.Triangulation(p * 2.0 ** k, seed=1).edges(), want), k
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_insertion_order_free_on_exact_ties(oracle, dim):
+    # every in-sphere test between points of one shell is an exact tie, decided
+    # by the perturbation by vertex id; the triangulation is still unique, so
+    # the reference's parallel path (another insertion order, same ids) and the
+    # sequential one agree, and the result passes the oracle's validator
+    p = _shells(dim)
+    a = oracle.Triangulation(p, seed=3)
+    b = oracle.Triangulation(p, seed=3, threads=4, prefix=len(p) // 5)
+    assert a.status == 0 and b.status == 0
+    assert np.array_equal(a.edges(), b.edges())
+    v, nb = a.simplices()
+    res = oracle.validate(dim, a.vertices(), v, nb, expect_vertices=len(p) + dim + 1)
+    assert res["non_positive"] == 0 and res["asymmetric"] == 0
+    assert res["not_perturbed_delaunay"] == 0 and res["missing_vertices"] == 0
